@@ -1,0 +1,120 @@
+/*
+ * vkhel extensions for GB300 -- declared beside the reference API.
+ *
+ * Everything here is exported by the same version script as the reference
+ * API (every vkhel_* symbol is global).  None of it has a counterpart in the
+ * reference's public header except where a line says so; the reference
+ * reports failures through assert() only and has no batched or asynchronous
+ * entry points.
+ */
+#ifndef VKHEL_EXT_H
+#define VKHEL_EXT_H
+
+#include "vkhel.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+enum vkhel_status {
+	VKHEL_OK = 0,
+	VKHEL_ERR_INVALID_ARGUMENT = 1, /* bad size, modulus, length or mismatched context */
+	VKHEL_ERR_OUT_OF_MEMORY = 2,    /* device or pinned allocation failed */
+	VKHEL_ERR_BUDGET = 3,           /* allocation would exceed the context budget */
+	VKHEL_ERR_DEVICE = 4,           /* a CUDA call failed */
+	VKHEL_ERR_NO_DEVICE = 5,        /* no CUDA device */
+	VKHEL_ERR_TIMEOUT = 6,          /* a bounded wait ran out */
+	VKHEL_ERR_CANCELLED = 7,        /* request cancelled before it ran */
+	VKHEL_ERR_UNSUPPORTED = 8       /* valid request this build does not run */
+};
+
+/* ---- context ---- */
+/* Status of the most recent failed call on this context (VKHEL_OK if none)
+ * and its message (copied into msg[0..len)).  Calls made with a NULL context,
+ * such as vkhel_ntt_tables_create, record into a per-thread slot read with
+ * ctx == NULL. */
+int vkhel_ctx_last_error(const struct vkhel_ctx *ctx, char *msg, size_t len);
+void vkhel_ctx_clear_error(struct vkhel_ctx *ctx);
+/* Device-memory budget in bytes for vectors and tables of this context
+ * (0 = unlimited, the default; VKHEL_DEVICE_BUDGET sets it at creation). */
+int vkhel_ctx_set_budget(struct vkhel_ctx *ctx, uint64_t bytes);
+uint64_t vkhel_ctx_bytes_in_use(const struct vkhel_ctx *ctx);
+/* The context's cudaStream_t, for interop and event timing. */
+void *vkhel_ctx_stream(struct vkhel_ctx *ctx);
+int vkhel_ctx_sync(struct vkhel_ctx *ctx);
+int vkhel_ctx_sm_count(const struct vkhel_ctx *ctx);
+/* Kernels launched by this library in this process (graph replays count
+ * each kernel node once per replay). */
+uint64_t vkhel_launch_count(void);
+
+/* ---- vectors ---- */
+uint64_t vkhel_vector_length(const struct vkhel_vector *v);
+/* Device address of the vector's words (CUDA device pointer). */
+uint64_t *vkhel_vector_device_ptr(struct vkhel_vector *v);
+/* Synchronous copies of `count` words between host memory and the start of
+ * the vector (count <= length). */
+int vkhel_vector_upload(struct vkhel_vector *v, const uint64_t *src, uint64_t count);
+int vkhel_vector_download(const struct vkhel_vector *v, uint64_t *dst, uint64_t count);
+/* Print the vector (reference: src/vector.c:237-247, exported there through
+ * the vkhel_* glob of vkhel.syms). */
+void vkhel_vector_dbgprint(const struct vkhel_vector *v);
+
+/* ---- tables ---- */
+/* Copy the host tables out (n words each; any pointer may be NULL). */
+int vkhel_ntt_tables_copy(const struct vkhel_ntt_tables *t, uint64_t *roots,
+		uint64_t *inv_roots, uint64_t *roots_shoup, uint64_t *inv_roots_shoup);
+/* Reference: src/ntt_tables.c:46-63. */
+void vkhel_ntt_tables_dbgprint(struct vkhel_ntt_tables *t);
+
+/* ---- arithmetic ---- */
+/* (a * multiplier + b) mod `mod`, canonical, for every 64-bit input: what
+ * vkhel_vector_elemfma computes whenever the reference shader's wrap-around
+ * (elemfma.comp:47-52) does not trigger. */
+void vkhel_vector_elemfma_canonical(const struct vkhel_vector *a,
+		const struct vkhel_vector *b, struct vkhel_vector *result,
+		uint64_t multiplier, uint64_t mod);
+/* Negacyclic product result = a * b mod (X^n + 1, q) of the first n words,
+ * equal to the reference composition forward(a), forward(b), elemmul,
+ * inverse.  One fused launch for 256 <= n <= 16384.  Returns a status. */
+int vkhel_vector_polymul(const struct vkhel_vector *a,
+		const struct vkhel_vector *b, struct vkhel_vector *result,
+		struct vkhel_ntt_tables *ntt);
+
+/* ---- batched polynomial multiply ----
+ * A batch is a fixed list of limb products, built once, committed (the job
+ * table is uploaded and, with VKHEL_BATCH_GRAPH, the launch sequence is
+ * captured in a CUDA graph), then launched any number of times.  Jobs of
+ * different degrees may be mixed; each degree class runs in its own kernel
+ * inside the same graph.  Operand memory is read at launch time, so new data
+ * in the same vectors is picked up by every launch. */
+struct vkhel_batch;
+enum vkhel_batch_flags {
+	VKHEL_BATCH_GRAPH = 1   /* capture and replay a CUDA graph */
+};
+struct vkhel_batch *vkhel_batch_create(struct vkhel_ctx *ctx);
+/* Add `limbs` limb products of one RNS polynomial: limb k uses tables[k] and
+ * the n words at offset k * n of a, b and c (vectors of >= limbs * n words). */
+int vkhel_batch_add_polymul(struct vkhel_batch *batch,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *a, const struct vkhel_vector *b,
+		struct vkhel_vector *c);
+/* Same with raw device pointers (32-byte aligned, limb-major). */
+int vkhel_batch_add_polymul_raw(struct vkhel_batch *batch,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b, uint64_t *c);
+int vkhel_batch_commit(struct vkhel_batch *batch, uint32_t flags);
+/* Enqueue one run on the context stream and return (asynchronous). */
+int vkhel_batch_launch(struct vkhel_batch *batch);
+/* Launch and wait. */
+int vkhel_batch_run(struct vkhel_batch *batch);
+uint32_t vkhel_batch_jobs(const struct vkhel_batch *batch);
+/* Kernels one launch of the batch issues. */
+uint32_t vkhel_batch_kernels(const struct vkhel_batch *batch);
+void vkhel_batch_destroy(struct vkhel_batch *batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

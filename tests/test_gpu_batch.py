@@ -1,0 +1,97 @@
+"""Batched polynomial multiply (vkhel_batch_*) against the oracle.
+
+Covers equal-degree RNS batches in one fused launch, ragged batches mixing
+degrees (fused classes and composed classes for n < 256 and n > 2^14),
+results aliasing an operand, CUDA-graph replay picking up new operand data,
+and the eager (non-graph) path.  Every limb product must equal the
+reference composition forward, forward, elemmul, inverse bit for bit.
+"""
+import numpy as np
+import pytest
+
+from vkhel_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(oracle, qs, ws, a_h, b_h, c_h, n):
+    for k, (q, w) in enumerate(zip(qs, ws)):
+        ref, st = oracle.polymul(a_h[k * n:(k + 1) * n], b_h[k * n:(k + 1) * n], n, q, w)
+        assert st == 0
+        np.testing.assert_array_equal(c_h[k * n:(k + 1) * n], ref, err_msg=f"limb {k}")
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_rns_batch(vk, ctx, oracle, graph):
+    n, limbs, pairs = 4096, 3, 5
+    qs, ws, a, b = workloads.rns_batch(n, limbs, pairs, seed=9)
+    tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+    batch = vk.Batch(ctx)
+    vecs = []
+    for i in range(pairs):
+        va, vb = vk.Vector(ctx, a[i].ravel()), vk.Vector(ctx, b[i].ravel())
+        vc = vk.Vector(ctx, limbs * n)
+        batch.add_polymul(tabs, va, vb, vc)
+        vecs.append((va, vb, vc))
+    batch.commit(graph=graph)
+    assert batch.jobs == pairs * limbs and batch.kernels >= 1
+    before = vk.launch_count()
+    batch.run()
+    assert vk.launch_count() - before == batch.kernels
+    for i, (va, vb, vc) in enumerate(vecs):
+        _check(oracle, qs, ws, a[i].ravel(), b[i].ravel(), vc.download(), n)
+    # new operand data in the same vectors is picked up by the next launch
+    rng = np.random.default_rng(77)
+    a2 = np.stack([workloads.uniform(rng, q, n) for q in qs]).ravel()
+    vecs[0][0].upload(a2)
+    batch.run()
+    _check(oracle, qs, ws, a2, b[0].ravel(), vecs[0][2].download(), n)
+
+
+def test_ragged_batch_mixes_degrees_and_aliasing(vk, ctx, oracle):
+    rng = np.random.default_rng(5)
+    batch = vk.Batch(ctx)
+    cases = []
+    for log_n, limbs, alias in [(4, 2, False), (9, 1, True), (12, 3, False), (14, 2, True), (15, 1, False),
+                                (13, 2, False), (12, 1, True), (16, 1, True), (7, 4, False)]:
+        n = 1 << log_n
+        qs = workloads.ntt_primes(n, limbs)
+        ws = [workloads.root_for(n, q) for q in qs]
+        tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+        a_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+        b_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+        va, vb = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h)
+        vc = va if alias else vk.Vector(ctx, limbs * n)
+        batch.add_polymul(tabs, va, vb, vc)
+        cases.append((qs, ws, a_h, b_h, vc, n, tabs, va, vb))
+    batch.commit(graph=True)
+    batch.run()
+    for qs, ws, a_h, b_h, vc, n, *_ in cases:
+        _check(oracle, qs, ws, a_h, b_h, vc.download(), n)
+
+
+def test_batch_raw_device_pointers(vk, ctx, oracle):
+    n, limbs = 8192, 2
+    qs, ws, a, b = workloads.rns_batch(n, limbs, 1, seed=4)
+    tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+    va, vb, vc = vk.Vector(ctx, a[0].ravel()), vk.Vector(ctx, b[0].ravel()), vk.Vector(ctx, limbs * n)
+    batch = vk.Batch(ctx)
+    batch.add_polymul(tabs, va.device_ptr, vb.device_ptr, vc.device_ptr)
+    batch.commit(graph=True)
+    batch.run()
+    _check(oracle, qs, ws, a[0].ravel(), b[0].ravel(), vc.download(), n)
+
+
+def test_batch_rejects_bad_input(vk, ctx):
+    n = 1024
+    q = workloads.ntt_primes(n, 1)[0]
+    t = vk.NttTables(n, q, workloads.root_for(n, q))
+    batch = vk.Batch(ctx)
+    short = vk.Vector(ctx, n - 1)
+    ok = vk.Vector(ctx, n)
+    with pytest.raises(vk.VkhelError):
+        batch.add_polymul([t], short, ok, ok)
+    with pytest.raises(vk.VkhelError):
+        batch.commit()  # empty
+    with pytest.raises(vk.VkhelError):
+        batch.launch()  # not committed

@@ -1,0 +1,369 @@
+"""vkhel_gb300: Python host mirror of the vkhel C API on GB300.
+
+The product is ``libvkhel.so`` (C host layer + sm_103a CUDA kernels, built by
+``vkhel_gb300.build``).  This module binds it with ctypes and mirrors the
+reference's API objects one to one:
+
+    reference (include/vkhel/vkhel.h)      here
+    vkhel_ctx_create / _destroy            Context()
+    vkhel_ntt_tables_create / _destroy     NttTables(n, q, w)
+    vkhel_vector_create / create2 / ...    Vector(ctx, length, zero=True)
+    vkhel_vector_elemfma / elemmod / ...   Vector methods and module functions
+
+Operations are synchronous like the reference's.  Errors that the reference
+turns into assert() aborts raise VkhelError here, carrying the library's
+status code and message.  There is no fallback: if the library is missing,
+importing ``lib()`` raises.
+"""
+import ctypes
+import os
+import weakref
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libvkhel.so")
+
+u64 = ctypes.c_uint64
+u32 = ctypes.c_uint32
+vp = ctypes.c_void_p
+P64 = ctypes.POINTER(ctypes.c_uint64)
+
+# (name, restype, argtypes) for every exported function of include/vkhel/*.h
+_SIGNATURES = [
+    ("vkhel_ctx_create", vp, []),
+    ("vkhel_ctx_destroy", None, [vp]),
+    ("vkhel_ntt_tables_create", vp, [u64, u64, u64]),
+    ("vkhel_ntt_tables_destroy", None, [vp]),
+    ("vkhel_vector_create", vp, [vp, u64]),
+    ("vkhel_vector_create2", vp, [vp, u64, ctypes.c_bool]),
+    ("vkhel_vector_destroy", None, [vp]),
+    ("vkhel_vector_dup", vp, [vp]),
+    ("vkhel_vector_copy_from_host", None, [vp, vp]),
+    ("vkhel_vector_map", None, [vp, ctypes.POINTER(vp), ctypes.c_size_t]),
+    ("vkhel_vector_unmap", None, [vp]),
+    ("vkhel_vector_elemfma", None, [vp, vp, vp, u64, u64]),
+    ("vkhel_vector_elemmod", None, [vp, vp, u64, u64]),
+    ("vkhel_vector_elemmul", None, [vp, vp, vp, u64]),
+    ("vkhel_vector_elemgtadd", None, [vp, vp, u64, u64]),
+    ("vkhel_vector_elemgtsub", None, [vp, vp, u64, u64, u64]),
+    ("vkhel_vector_forward_transform", None, [vp, vp, vp]),
+    ("vkhel_vector_inverse_transform", None, [vp, vp, vp]),
+    # extensions
+    ("vkhel_ctx_last_error", ctypes.c_int, [vp, ctypes.c_char_p, ctypes.c_size_t]),
+    ("vkhel_ctx_clear_error", None, [vp]),
+    ("vkhel_ctx_set_budget", ctypes.c_int, [vp, u64]),
+    ("vkhel_ctx_bytes_in_use", u64, [vp]),
+    ("vkhel_ctx_stream", vp, [vp]),
+    ("vkhel_ctx_sync", ctypes.c_int, [vp]),
+    ("vkhel_ctx_sm_count", ctypes.c_int, [vp]),
+    ("vkhel_launch_count", u64, []),
+    ("vkhel_vector_length", u64, [vp]),
+    ("vkhel_vector_device_ptr", vp, [vp]),
+    ("vkhel_vector_upload", ctypes.c_int, [vp, vp, u64]),
+    ("vkhel_vector_download", ctypes.c_int, [vp, vp, u64]),
+    ("vkhel_vector_dbgprint", None, [vp]),
+    ("vkhel_ntt_tables_copy", ctypes.c_int, [vp, vp, vp, vp, vp]),
+    ("vkhel_ntt_tables_dbgprint", None, [vp]),
+    ("vkhel_vector_elemfma_canonical", None, [vp, vp, vp, u64, u64]),
+    ("vkhel_vector_polymul", ctypes.c_int, [vp, vp, vp, vp]),
+    ("vkhel_batch_create", vp, [vp]),
+    ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_batch_commit", ctypes.c_int, [vp, u32]),
+    ("vkhel_batch_launch", ctypes.c_int, [vp]),
+    ("vkhel_batch_run", ctypes.c_int, [vp]),
+    ("vkhel_batch_jobs", u32, [vp]),
+    ("vkhel_batch_kernels", u32, [vp]),
+    ("vkhel_batch_destroy", None, [vp]),
+]
+
+STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "BUDGET", 4: "DEVICE",
+          5: "NO_DEVICE", 6: "TIMEOUT", 7: "CANCELLED", 8: "UNSUPPORTED"}
+BATCH_GRAPH = 1
+
+_lib = None
+
+
+class VkhelError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"vkhel {STATUS.get(code, code)}: {msg}")
+        self.code = code
+        self.msg = msg
+
+
+def lib(path=None):
+    """Load libvkhel.so (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or os.environ.get("VKHEL_LIB", LIB_PATH)
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} missing: build it with `python -m vkhel_gb300.build`")
+    L = ctypes.CDLL(p)
+    for name, res, args in _SIGNATURES:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def last_error(ctx_ptr=None):
+    buf = ctypes.create_string_buffer(256)
+    code = lib().vkhel_ctx_last_error(ctx_ptr, buf, 256)
+    return code, buf.value.decode(errors="replace")
+
+
+def _check_ctx(ctx_ptr):
+    code, msg = last_error(ctx_ptr)
+    if code:
+        lib().vkhel_ctx_clear_error(ctx_ptr)
+        raise VkhelError(code, msg)
+
+
+def _status(ctx_ptr, code):
+    if code:
+        _, msg = last_error(ctx_ptr)
+        lib().vkhel_ctx_clear_error(ctx_ptr)
+        raise VkhelError(code, msg)
+
+
+def _as_u64(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint64))
+
+
+class Context:
+    """vkhel_ctx: one CUDA device, stream and device pool."""
+
+    def __init__(self):
+        L = lib()
+        L.vkhel_ctx_clear_error(None)
+        self.ptr = L.vkhel_ctx_create()
+        if not self.ptr:
+            code, msg = last_error(None)
+            raise VkhelError(code or 5, msg)
+        self._children = weakref.WeakSet()
+
+    def close(self):
+        if self.ptr:
+            for ch in list(self._children):
+                ch.close()
+            lib().vkhel_ctx_destroy(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return lib().vkhel_ctx_stream(self.ptr)
+
+    @property
+    def sm_count(self):
+        return lib().vkhel_ctx_sm_count(self.ptr)
+
+    def sync(self):
+        _status(self.ptr, lib().vkhel_ctx_sync(self.ptr))
+
+    def set_budget(self, nbytes):
+        _status(self.ptr, lib().vkhel_ctx_set_budget(self.ptr, int(nbytes)))
+
+    @property
+    def bytes_in_use(self):
+        return lib().vkhel_ctx_bytes_in_use(self.ptr)
+
+    def vector(self, length_or_data, zero=True):
+        return Vector(self, length_or_data, zero)
+
+
+class NttTables:
+    """vkhel_ntt_tables for degree n, modulus q, primitive 2n-th root w."""
+
+    def __init__(self, n, q, w):
+        L = lib()
+        L.vkhel_ctx_clear_error(None)
+        self.n, self.q, self.w = int(n), int(q), int(w)
+        self.ptr = L.vkhel_ntt_tables_create(self.n, self.q, self.w)
+        if not self.ptr:
+            code, msg = last_error(None)
+            raise VkhelError(code or 1, msg)
+
+    def arrays(self):
+        out = [np.zeros(self.n, dtype=np.uint64) for _ in range(4)]
+        lib().vkhel_ntt_tables_copy(self.ptr, *[o.ctypes.data for o in out])
+        return dict(zip(("roots", "inv_roots", "roots_shoup", "inv_roots_shoup"), out))
+
+    def close(self):
+        if self.ptr:
+            lib().vkhel_ntt_tables_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Vector:
+    """vkhel_vector: `length` device-resident uint64 words."""
+
+    def __init__(self, ctx, length_or_data, zero=True):
+        L = lib()
+        self.ctx = ctx
+        data = None
+        if np.ndim(length_or_data) > 0:
+            data = _as_u64(length_or_data)
+            length = data.size
+            zero = False
+        else:
+            length = int(length_or_data)
+        self.ptr = L.vkhel_vector_create2(ctx.ptr, length, bool(zero))
+        if not self.ptr:
+            _check_ctx(ctx.ptr)
+            raise VkhelError(2, "vector_create failed")
+        self.length = length
+        ctx._children.add(self)
+        if data is not None:
+            self.upload(data)
+
+    @classmethod
+    def _wrap(cls, ctx, ptr, length):
+        v = cls.__new__(cls)
+        v.ctx, v.ptr, v.length = ctx, ptr, length
+        ctx._children.add(v)
+        return v
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().vkhel_vector_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_ptr(self):
+        return lib().vkhel_vector_device_ptr(self.ptr)
+
+    def upload(self, data):
+        data = _as_u64(data)
+        _status(self.ctx.ptr, lib().vkhel_vector_upload(self.ptr, data.ctypes.data, data.size))
+
+    def copy_from_host(self, data):
+        data = _as_u64(data)
+        assert data.size >= self.length
+        lib().vkhel_vector_copy_from_host(self.ptr, data.ctypes.data)
+        _check_ctx(self.ctx.ptr)
+
+    def download(self, count=None):
+        count = self.length if count is None else count
+        out = np.empty(count, dtype=np.uint64)
+        _status(self.ctx.ptr, lib().vkhel_vector_download(self.ptr, out.ctypes.data, count))
+        return out
+
+    def map_read(self, size=None):
+        """Contents through vkhel_vector_map / unmap (the reference's path)."""
+        size = self.length * 8 if size is None else size
+        p = vp()
+        L = lib()
+        L.vkhel_vector_map(self.ptr, ctypes.byref(p), size)
+        _check_ctx(self.ctx.ptr)
+        out = np.ctypeslib.as_array(ctypes.cast(p, P64), shape=(self.length,)).copy() if self.length else \
+            np.empty(0, np.uint64)
+        L.vkhel_vector_unmap(self.ptr)
+        _check_ctx(self.ctx.ptr)
+        return out
+
+    def dup(self):
+        p = lib().vkhel_vector_dup(self.ptr)
+        if not p:
+            _check_ctx(self.ctx.ptr)
+        return Vector._wrap(self.ctx, p, self.length)
+
+
+def _op(name, *args):
+    getattr(lib(), name)(*[a.ptr if isinstance(a, (Vector, NttTables)) else a for a in args])
+    ctx = next(a.ctx for a in args if isinstance(a, Vector))
+    _check_ctx(ctx.ptr)
+
+
+def elemfma(a, b, res, multiplier, mod): _op("vkhel_vector_elemfma", a, b, res, int(multiplier), int(mod))
+def elemfma_canonical(a, b, res, multiplier, mod): _op("vkhel_vector_elemfma_canonical", a, b, res, int(multiplier), int(mod))
+def elemmod(a, res, mod, q): _op("vkhel_vector_elemmod", a, res, int(mod), int(q))
+def elemmul(a, b, res, mod): _op("vkhel_vector_elemmul", a, b, res, int(mod))
+def elemgtadd(a, res, bound, diff): _op("vkhel_vector_elemgtadd", a, res, int(bound), int(diff))
+def elemgtsub(a, res, bound, diff, mod): _op("vkhel_vector_elemgtsub", a, res, int(bound), int(diff), int(mod))
+def forward_transform(a, res, tables): _op("vkhel_vector_forward_transform", a, res, tables)
+def inverse_transform(a, res, tables): _op("vkhel_vector_inverse_transform", a, res, tables)
+
+
+def polymul(a, b, res, tables):
+    _status(res.ctx.ptr, lib().vkhel_vector_polymul(a.ptr, b.ptr, res.ptr, tables.ptr))
+
+
+def launch_count():
+    return lib().vkhel_launch_count()
+
+
+class Batch:
+    """vkhel_batch: a committed list of limb products launched as one unit."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.ptr = lib().vkhel_batch_create(ctx.ptr)
+        if not self.ptr:
+            _check_ctx(ctx.ptr)
+        self._keep = []
+        ctx._children.add(self)
+
+    def add_polymul(self, tables, a, b, c):
+        arr = (vp * len(tables))(*[t.ptr for t in tables])
+        self._keep.append(tables)
+        if isinstance(a, Vector):
+            code = lib().vkhel_batch_add_polymul(self.ptr, arr, len(tables), a.ptr, b.ptr, c.ptr)
+        else:  # raw device pointers
+            code = lib().vkhel_batch_add_polymul_raw(self.ptr, arr, len(tables), int(a), int(b), int(c))
+        _status(self.ctx.ptr, code)
+
+    def commit(self, graph=True):
+        _status(self.ctx.ptr, lib().vkhel_batch_commit(self.ptr, BATCH_GRAPH if graph else 0))
+
+    def launch(self):
+        _status(self.ctx.ptr, lib().vkhel_batch_launch(self.ptr))
+
+    def run(self):
+        _status(self.ctx.ptr, lib().vkhel_batch_run(self.ptr))
+
+    @property
+    def jobs(self):
+        return lib().vkhel_batch_jobs(self.ptr)
+
+    @property
+    def kernels(self):
+        return lib().vkhel_batch_kernels(self.ptr)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().vkhel_batch_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

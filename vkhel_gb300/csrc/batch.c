@@ -1,0 +1,306 @@
+/*
+ * Batched polynomial multiply (no counterpart in the reference, whose callers
+ * compose forward(a), forward(b), elemmul, inverse one blocking call at a
+ * time: 3 log2(n) + 2 submits per limb product).
+ *
+ * A batch records limb jobs, then commit():
+ *   - sorts the jobs by degree into classes and uploads one device job table;
+ *   - gives every job that needs it an n-word scratch slice (NTT(b) parking
+ *     when c aliases a, or the composed path for n outside the fused range);
+ *   - optionally captures the class launches into a CUDA graph (one fused
+ *     persistent kernel per class for 256 <= n <= 16384; forward, forward,
+ *     pointwise, inverse kernels over the whole class otherwise).
+ * launch() replays the graph (or re-issues the launches) on the context
+ * stream without waiting.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "internal.h"
+
+#define MAX_CLASSES 32
+
+struct job_rec {
+	uint32_t log_n;
+	uint32_t needs_scratch;
+	vkcu_poly_job job;
+};
+
+struct job_class {
+	uint32_t log_n;
+	uint32_t first, count;
+	int fused;
+};
+
+struct vkhel_batch {
+	struct vkhel_ctx *ctx;
+	struct job_rec *recs;
+	uint32_t njobs, cap;
+	int committed;
+	uint32_t flags;
+	struct job_class classes[MAX_CLASSES];
+	uint32_t nclasses;
+	void *dev;             /* poly jobs, then 3 ntt-job arrays per composed class */
+	uint64_t dev_bytes;
+	void *scratch;
+	uint64_t scratch_bytes;
+	vkcu_poly_job *dev_poly;
+	vkcu_ntt_job *dev_ntt; /* [3 * njobs]: b->scratch, a->c, c->c */
+	void *graph;
+	uint32_t kernels;
+};
+
+struct vkhel_batch *vkhel_batch_create(struct vkhel_ctx *ctx) {
+	if (!ctx) {
+		vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_create: NULL context");
+		return NULL;
+	}
+	struct vkhel_batch *b = calloc(1, sizeof(*b));
+	if (!b)
+		vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "batch_create: host allocation failed");
+	else
+		b->ctx = ctx;
+	return b;
+}
+
+static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *bb, uint64_t *c) {
+	struct vkhel_ctx *ctx = b->ctx;
+	if (b->committed)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch: already committed");
+	if (!tables || limbs == 0 || !a || !bb || !c)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: bad arguments");
+	if (((uintptr_t) a | (uintptr_t) bb | (uintptr_t) c) & 31)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: pointers must be 32-byte aligned");
+	const uint64_t n = tables[0] ? tables[0]->n : 0;
+	for (uint32_t k = 0; k < limbs; k++) {
+		const struct vkhel_ntt_tables *t = tables[k];
+		if (!t || t->n != n || n < 2)
+			return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: limb %u tables invalid", k);
+		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_fused_log_n() + 4)
+			return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_add: limb %u (n, q) unsupported", k);
+	}
+	if (b->njobs + limbs > b->cap) {
+		uint32_t cap = b->cap ? b->cap : 64;
+		while (cap < b->njobs + limbs)
+			cap *= 2;
+		struct job_rec *r = realloc(b->recs, sizeof(*r) * cap);
+		if (!r)
+			return vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "batch_add: host allocation failed");
+		b->recs = r;
+		b->cap = cap;
+	}
+	for (uint32_t k = 0; k < limbs; k++) {
+		const struct vkh_devtab *d = NULL;
+		const int st = vkh_devtab_get(ctx, tables[k], &d);
+		if (st)
+			return st;
+		struct job_rec *r = &b->recs[b->njobs++];
+		const uint32_t log_n = tables[k]->log_n;
+		const int fused = log_n >= 8 && log_n <= vkcu_max_fused_log_n();
+		const uint64_t *ak = a + (uint64_t) k * n, *bk = bb + (uint64_t) k * n;
+		uint64_t *ck = c + (uint64_t) k * n;
+		/* the fused kernel parks NTT(b) in c, which must not hold a */
+		const int overlap = ak < ck + n && ck < ak + n;
+		r->log_n = log_n;
+		r->needs_scratch = !fused || overlap;
+		r->job.a = ak;
+		r->job.b = bk;
+		r->job.c = ck;
+		r->job.scratch = ck;
+		r->job.tw = d->dev_set;
+	}
+	return VKHEL_OK;
+}
+
+int vkhel_batch_add_polymul(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *a, const struct vkhel_vector *bb, struct vkhel_vector *c) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
+	if (!a || !bb || !c || !tables || !tables[0])
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL argument");
+	if (a->ctx != b->ctx || bb->ctx != b->ctx || c->ctx != b->ctx)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors of another context");
+	const uint64_t need = (uint64_t) limbs * tables[0]->n;
+	if (a->length < need || bb->length < need || c->length < need)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors shorter than limbs * n");
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev);
+}
+
+int vkhel_batch_add_polymul_raw(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *bb, uint64_t *c) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
+	return add_jobs(b, tables, limbs, a, bb, c);
+}
+
+static int cmp_rec(const void *x, const void *y) {
+	const struct job_rec *a = x, *b = y;
+	return (a->log_n > b->log_n) - (a->log_n < b->log_n);
+}
+
+/* Issue every class of the batch on the context stream. */
+static int issue(struct vkhel_batch *b) {
+	struct vkhel_ctx *ctx = b->ctx;
+	for (uint32_t k = 0; k < b->nclasses; k++) {
+		const struct job_class *cl = &b->classes[k];
+		int e;
+		if (cl->fused) {
+			e = vkcu_polymul(ctx->stream, b->dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, ctx->sms);
+		} else {
+			vkcu_ntt_job *nj = b->dev_ntt + 3 * (size_t) cl->first;
+			e = vkcu_ntt_forward(ctx->stream, nj, (int) cl->count, NULL, cl->log_n, ctx->sms);
+			if (!e)
+				e = vkcu_ntt_forward(ctx->stream, nj + cl->count, (int) cl->count, NULL, cl->log_n, ctx->sms);
+			if (!e)
+				e = vkcu_pointwise(ctx->stream, b->dev_poly + cl->first, (int) cl->count, cl->log_n, ctx->sms);
+			if (!e)
+				e = vkcu_ntt_inverse(ctx->stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n,
+						ctx->sms);
+		}
+		if (e)
+			return e;
+	}
+	return 0;
+}
+
+int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_commit: NULL batch");
+	struct vkhel_ctx *ctx = b->ctx;
+	if (b->committed)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_commit: already committed");
+	if (b->njobs == 0)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_commit: empty batch");
+	qsort(b->recs, b->njobs, sizeof(*b->recs), cmp_rec);
+
+	/* classes and scratch slices */
+	uint64_t scratch_words = 0;
+	b->nclasses = 0;
+	for (uint32_t i = 0; i < b->njobs; i++) {
+		struct job_rec *r = &b->recs[i];
+		if (b->nclasses == 0 || b->classes[b->nclasses - 1].log_n != r->log_n) {
+			if (b->nclasses == MAX_CLASSES)
+				return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_commit: too many degree classes");
+			struct job_class *cl = &b->classes[b->nclasses++];
+			cl->log_n = r->log_n;
+			cl->first = i;
+			cl->count = 0;
+			cl->fused = r->log_n >= 8 && r->log_n <= vkcu_max_fused_log_n();
+		}
+		b->classes[b->nclasses - 1].count++;
+		if (r->needs_scratch)
+			scratch_words += (uint64_t) 1 << r->log_n;
+	}
+	if (scratch_words) {
+		b->scratch_bytes = scratch_words * sizeof(uint64_t);
+		int st = vkh_dev_alloc(ctx, b->scratch_bytes, &b->scratch);
+		if (st)
+			return st;
+		uint64_t off = 0;
+		for (uint32_t i = 0; i < b->njobs; i++) {
+			struct job_rec *r = &b->recs[i];
+			if (r->needs_scratch) {
+				r->job.scratch = (uint64_t *) b->scratch + off;
+				off += (uint64_t) 1 << r->log_n;
+			}
+		}
+	}
+
+	/* device job table: poly jobs, then per composed class 3 ntt-job arrays
+	 * laid out at 3 * first (so every class indexes its own slice) */
+	const uint64_t poly_bytes = sizeof(vkcu_poly_job) * b->njobs;
+	const uint64_t ntt_off = (poly_bytes + 255) & ~(uint64_t) 255;
+	b->dev_bytes = ntt_off + sizeof(vkcu_ntt_job) * 3 * (uint64_t) b->njobs;
+	void *host = calloc(1, b->dev_bytes);
+	if (!host)
+		return vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "batch_commit: host allocation failed");
+	vkcu_poly_job *hp = host;
+	vkcu_ntt_job *hn = (vkcu_ntt_job *) ((char *) host + ntt_off);
+	for (uint32_t i = 0; i < b->njobs; i++)
+		hp[i] = b->recs[i].job;
+	for (uint32_t k = 0; k < b->nclasses; k++) {
+		const struct job_class *cl = &b->classes[k];
+		vkcu_ntt_job *nj = hn + 3 * (size_t) cl->first;
+		for (uint32_t i = 0; i < cl->count; i++) {
+			const vkcu_poly_job *j = &hp[cl->first + i];
+			nj[i] = (vkcu_ntt_job){j->b, j->scratch, j->tw};
+			nj[cl->count + i] = (vkcu_ntt_job){j->a, j->c, j->tw};
+			nj[2 * cl->count + i] = (vkcu_ntt_job){j->c, j->c, j->tw};
+		}
+	}
+	int st = vkh_dev_alloc(ctx, b->dev_bytes, &b->dev);
+	if (st) {
+		free(host);
+		return st;
+	}
+	int e = vkcu_h2d(ctx->stream, b->dev, host, b->dev_bytes);
+	if (!e)
+		e = vkcu_sync(ctx->stream);
+	free(host);
+	if (e)
+		return vkh_cuda(ctx, e, "batch_commit: job table upload");
+	b->dev_poly = b->dev;
+	b->dev_ntt = (vkcu_ntt_job *) ((char *) b->dev + ntt_off);
+
+	const uint64_t before = vkcu_launch_count();
+	if (flags & VKHEL_BATCH_GRAPH) {
+		e = vkcu_capture_begin(ctx->stream);
+		if (!e) {
+			const int ie = issue(b);
+			void *exec = NULL;
+			e = vkcu_capture_end(ctx->stream, &exec);
+			if (!e)
+				e = ie;
+			b->graph = exec;
+		}
+	} else {
+		e = issue(b); /* one eager run also validates the launches */
+		if (!e)
+			e = vkcu_sync(ctx->stream);
+	}
+	b->kernels = (uint32_t) (vkcu_launch_count() - before);
+	if (flags & VKHEL_BATCH_GRAPH)
+		vkcu_count_launches((uint64_t) 0 - b->kernels); /* capture executes nothing */
+	if (e)
+		return vkh_cuda(ctx, e, "batch_commit: launch");
+	b->flags = flags;
+	b->committed = 1;
+	return VKHEL_OK;
+}
+
+int vkhel_batch_launch(struct vkhel_batch *b) {
+	if (!b || !b->committed)
+		return vkh_fail(b ? b->ctx : NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_launch: not committed");
+	int e;
+	if (b->graph) {
+		e = vkcu_graph_launch(b->graph, b->ctx->stream);
+		if (!e)
+			vkcu_count_launches(b->kernels);
+	} else {
+		e = issue(b);
+	}
+	return vkh_cuda(b->ctx, e, "batch_launch");
+}
+
+int vkhel_batch_run(struct vkhel_batch *b) {
+	int st = vkhel_batch_launch(b);
+	if (st)
+		return st;
+	return vkh_cuda(b->ctx, vkcu_sync(b->ctx->stream), "batch_run");
+}
+
+uint32_t vkhel_batch_jobs(const struct vkhel_batch *b) { return b ? b->njobs : 0; }
+uint32_t vkhel_batch_kernels(const struct vkhel_batch *b) { return b ? b->kernels : 0; }
+
+void vkhel_batch_destroy(struct vkhel_batch *b) {
+	if (!b)
+		return;
+	struct vkhel_ctx *ctx = b->ctx;
+	vkcu_sync(ctx->stream);
+	vkcu_graph_destroy(b->graph);
+	vkh_dev_free(ctx, b->dev, b->dev_bytes);
+	vkh_dev_free(ctx, b->scratch, b->scratch_bytes);
+	free(b->recs);
+	free(b);
+}

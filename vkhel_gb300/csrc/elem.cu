@@ -1,0 +1,176 @@
+// Element-wise modular kernels for sm_103a.
+//
+// Each operation restates one reference shader with the constants its host
+// wrapper pushes, so results equal the reference's for every 64-bit input:
+//   elemmul        src/kernels/shaders/elemmul.comp:62-73      (elemmul.c:159-168)
+//   elemmulconst   src/kernels/shaders/elemmulconst.comp:35-49 (elemmulconst.c:154-163)
+//   elemfma        src/kernels/shaders/elemfma.comp:36-55      (elemfma.c:159-169)
+//   elemgtsub      src/kernels/shaders/elemgtsub.comp:49-67    (elemgtsub.c:154-168)
+//   elemgtadd      src/kernels/shaders/elemgtadd.comp:20-30
+//   elemmodbytwo   src/kernels/shaders/elemmodbytwo.comp:19-27
+// plus elemfma_canonical, the exact (a m + b) mod q.
+//
+// These are HBM-bound streams: each thread moves two words per operand with
+// 16-byte vector accesses, the grid is a multiple of the SM count and loops
+// grid-stride; one scalar tail element is handled by the last thread.
+#include <cuda_runtime.h>
+
+#include "arith.cuh"
+#include "kernels.h"
+
+namespace vk {
+
+struct OpMul {
+  u64 mod, mu;
+  u32 bits;
+  __device__ __forceinline__ u64 operator()(u64 a, u64 b) const {
+    const u64 x = ref_reduce64(a, mod, mu, bits);
+    const u64 y = ref_reduce64(b, mod, mu, bits);
+    return ref_reduce128(mulhi(x, y), x * y, mod, mu, bits);
+  }
+};
+
+struct OpMulConst {
+  u64 c, cs, mod;
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const { return shoup(a, c, cs, mod); }
+};
+
+// elemfma.comp:43-54 as written: both "reductions" compute mod - x.
+struct OpFmaRef {
+  u64 m, ms, mod;
+  __device__ __forceinline__ u64 operator()(u64 a, u64 b) const {
+    u64 p = a * m - mulhi(a, ms) * mod;
+    if (p >= mod) p = mod - p;
+    const u64 s = p + b;
+    return s >= mod ? mod - s : s;
+  }
+};
+
+// (a m + b) mod q for any 64-bit a, b; m is given reduced with its Shoup factor.
+struct OpFmaCanon {
+  u64 m, ms, mod, mu;
+  u32 bits;
+  __device__ __forceinline__ u64 operator()(u64 a, u64 b) const {
+    const u64 p = shoup(ref_reduce64(a, mod, mu, bits), m, ms, mod);
+    const u64 y = ref_reduce64(b, mod, mu, bits);
+    const u64 s = p + y;
+    return (s < p || s >= mod) ? s - mod : s;
+  }
+};
+
+struct OpGtSub {
+  u64 bound, d, mod, mu;
+  u32 bits;
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const {
+    const u64 r = ref_reduce64(a, mod, mu, bits);
+    if (a > bound) {
+      const u64 z = r + mod - d;
+      return z >= mod ? z - mod : z;
+    }
+    return r;
+  }
+};
+
+struct OpGtAdd {
+  u64 bound, diff;
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const { return a > bound ? a + diff : a; }
+};
+
+struct OpModTwo {
+  u64 sb;
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const {
+    const u64 bit = a & 1;
+    return a > sb ? 1 - bit : bit;
+  }
+};
+
+__device__ __forceinline__ ulonglong2 ld2(const u64* p) {
+  ulonglong2 r;
+  asm volatile("ld.global.L1::no_allocate.v2.u64 {%0,%1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ void st2(u64* p, u64 a, u64 b) {
+  asm volatile("st.global.v2.u64 [%0], {%1,%2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
+
+// B == nullptr for unary operations.
+template <class Op>
+__global__ void __launch_bounds__(256) k_elementwise(u64* __restrict__ res, const u64* a, const u64* b, u64 len,
+                                                     Op op) {
+  const u64 pairs = len >> 1;
+  const u64 stride = (u64)gridDim.x * blockDim.x;
+  for (u64 p = (u64)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += stride) {
+    const ulonglong2 x = ld2(a + 2 * p);
+    ulonglong2 y = make_ulonglong2(0, 0);
+    if (b) y = ld2(b + 2 * p);
+    st2(res + 2 * p, op(x.x, y.x), op(x.y, y.y));
+  }
+  if ((len & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    const u64 i = len - 1;
+    res[i] = op(a[i], b ? b[i] : 0ull);
+  }
+}
+
+static int g_sms = 0;
+
+template <class Op>
+static int launch(void* stream, uint64_t* res, const uint64_t* a, const uint64_t* b, uint64_t len, Op op) {
+  if (len == 0) return 0;
+  if (((reinterpret_cast<uintptr_t>(res) | reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) != 0)
+    return (int)cudaErrorMisalignedAddress;
+  if (g_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 1;
+  }
+  const u64 pairs = (len + 1) / 2;
+  u64 blocks = (pairs + 255) / 256;
+  const u64 cap = (u64)g_sms * 8;
+  if (blocks > cap) blocks = cap;
+  k_elementwise<Op><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<u64*>(res), reinterpret_cast<const u64*>(a), reinterpret_cast<const u64*>(b), len, op);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace vk
+
+using namespace vk;
+
+extern "C" int vkcu_elemmul(void* stream, uint64_t* res, const uint64_t* a, const uint64_t* b, uint64_t len,
+                            uint64_t mod, uint64_t mu, uint32_t bits) {
+  return launch(stream, res, a, b, len, OpMul{mod, mu, bits});
+}
+
+extern "C" int vkcu_elemmulconst(void* stream, uint64_t* res, const uint64_t* a, uint64_t len, uint64_t c,
+                                 uint64_t c_shoup, uint64_t mod) {
+  return launch(stream, res, a, nullptr, len, OpMulConst{c, c_shoup, mod});
+}
+
+extern "C" int vkcu_elemfma(void* stream, uint64_t* res, const uint64_t* a, const uint64_t* b, uint64_t len,
+                            uint64_t m, uint64_t m_shoup, uint64_t mod) {
+  return launch(stream, res, a, b, len, OpFmaRef{m, m_shoup, mod});
+}
+
+extern "C" int vkcu_elemfma_canonical(void* stream, uint64_t* res, const uint64_t* a, const uint64_t* b,
+                                      uint64_t len, uint64_t m_red, uint64_t m_shoup, uint64_t mod, uint64_t mu,
+                                      uint32_t bits) {
+  return launch(stream, res, a, b, len, OpFmaCanon{m_red, m_shoup, mod, mu, bits});
+}
+
+extern "C" int vkcu_elemgtsub(void* stream, uint64_t* res, const uint64_t* a, uint64_t len, uint64_t bound,
+                              uint64_t diff_red, uint64_t mod, uint64_t mu, uint32_t bits) {
+  return launch(stream, res, a, nullptr, len, OpGtSub{bound, diff_red, mod, mu, bits});
+}
+
+extern "C" int vkcu_elemgtadd(void* stream, uint64_t* res, const uint64_t* a, uint64_t len, uint64_t bound,
+                              uint64_t diff) {
+  return launch(stream, res, a, nullptr, len, OpGtAdd{bound, diff});
+}
+
+extern "C" int vkcu_elemmodbytwo(void* stream, uint64_t* res, const uint64_t* a, uint64_t len,
+                                 uint64_t signed_bound) {
+  return launch(stream, res, a, nullptr, len, OpModTwo{signed_bound});
+}

@@ -1,0 +1,76 @@
+/*
+ * Internal types of libvkhel's C host layer.
+ */
+#ifndef VKHEL_GB300_INTERNAL_H
+#define VKHEL_GB300_INTERNAL_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/vkhel/vkhel_ext.h"
+#include "kernels.h"
+
+/* Device copy of one (n, q, w) table set, cached in a context. */
+struct vkh_devtab {
+	struct vkh_devtab *next;
+	uint64_t n, q, w;
+	void *mem;                 /* pool allocation: twset struct + 2 tables */
+	uint64_t bytes;
+	const vkcu_twset *dev_set; /* device address of the twset struct */
+	vkcu_twset host_set;       /* same values, device pointers */
+};
+
+struct vkhel_ctx {
+	int device;
+	int sms;
+	void *stream;
+	void *pool;
+	uint64_t budget;           /* 0 = unlimited */
+	uint64_t in_use;
+	int strict;                /* abort on error like the reference's asserts */
+	int last_error;
+	char last_msg[256];
+	struct vkh_devtab *tabs;
+};
+
+struct vkhel_vector {
+	struct vkhel_ctx *ctx;
+	uint64_t length;
+	uint64_t *dev;
+	uint64_t bytes;            /* bytes charged to the context */
+	void *window;              /* pinned host window of map/unmap */
+	size_t window_bytes;
+	bool mapped;
+};
+
+struct vkhel_ntt_tables {
+	uint64_t n, q, w;
+	uint32_t log_n;
+	/* host arrays, the reference's layout (include/priv/ntt_tables.h:6-15) */
+	uint64_t *roots, *inv_roots, *roots_shoup, *inv_roots_shoup;
+	/* derived constants for the device twiddle set */
+	uint64_t mu, ninv, ninv_s, w1ninv, w1ninv_s;
+	uint32_t qbits;
+};
+
+/* numbers.c -- host number theory with the reference's formulas */
+uint64_t vkh_bitlen(uint64_t v);
+uint64_t vkh_shoup(uint64_t factor, uint64_t mod);
+uint64_t vkh_barrett_mu(uint64_t mod);
+uint64_t vkh_ref_reduce64(uint64_t x, uint64_t mod, uint64_t mu);
+uint64_t vkh_mulmod(uint64_t a, uint64_t b, uint64_t mod);
+uint64_t vkh_powmod(uint64_t base, uint64_t exp, uint64_t mod);
+uint64_t vkh_invmod(uint64_t a, uint64_t mod);
+
+/* api.c -- error reporting; returns `code` */
+int vkh_fail(struct vkhel_ctx *ctx, int code, const char *fmt, ...);
+int vkh_cuda(struct vkhel_ctx *ctx, int cuda_err, const char *what);
+int vkh_dev_alloc(struct vkhel_ctx *ctx, uint64_t bytes, void **ptr);
+void vkh_dev_free(struct vkhel_ctx *ctx, void *ptr, uint64_t bytes);
+/* tables.c -- device table cache */
+int vkh_devtab_get(struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t,
+		const struct vkh_devtab **out);
+void vkh_devtab_release_all(struct vkhel_ctx *ctx);
+
+#endif

@@ -1,0 +1,112 @@
+/*
+ * C ABI between the C host library (api.c, tables.c) and the CUDA side
+ * (runtime.cu, elem.cu, ntt.cu).  Plain pointers and sizes only.  These
+ * symbols are internal to libvkhel.so (the version script exports vkhel_*
+ * only).
+ */
+#ifndef VKHEL_GB300_KERNELS_H
+#define VKHEL_GB300_KERNELS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Device-resident constants of one (n, q, w) twiddle set.  `fwd` and `inv`
+ * point to n interleaved (root, shoup(root)) pairs in the reference's
+ * bit-reversed order (src/ntt_tables.c:25-43). */
+typedef struct vkcu_twset {
+	uint64_t q, q2, mu;          /* q, 2q, floor(2^(bits+62)/q) */
+	uint64_t ninv, ninv_s;       /* n^-1 mod q and its Shoup factor */
+	uint64_t w1ninv, w1ninv_s;   /* inv_roots[1] * n^-1 mod q and Shoup factor */
+	uint32_t qbits, log_n;
+	const uint64_t *fwd;
+	const uint64_t *inv;
+} vkcu_twset;
+
+/* One transform of one vector.  The transform reads n words at `in` and
+ * writes n words at `out` (which may equal `in`). */
+typedef struct vkcu_ntt_job {
+	const uint64_t *in;
+	uint64_t *out;
+	const vkcu_twset *tw;        /* device pointer */
+} vkcu_ntt_job;
+
+/* One negacyclic limb product c = a * b mod (X^n + 1, q).  `scratch` holds n
+ * words for NTT(b) during the kernel; it may be `c` unless c overlaps a. */
+typedef struct vkcu_poly_job {
+	const uint64_t *a;
+	const uint64_t *b;
+	uint64_t *c;
+	uint64_t *scratch;
+	const vkcu_twset *tw;        /* device pointer */
+} vkcu_poly_job;
+
+/* ---- runtime (runtime.cu) ---- */
+int vkcu_device_count(int *count);
+int vkcu_set_device(int device);
+int vkcu_sm_count(int device, int *sms);
+int vkcu_stream_create(void **stream);
+int vkcu_stream_destroy(void *stream);
+int vkcu_pool_create(int device, void **pool);
+int vkcu_pool_destroy(void *pool);
+int vkcu_alloc(void *pool, void *stream, size_t bytes, void **ptr);
+int vkcu_free(void *stream, void *ptr);
+int vkcu_memset0(void *stream, void *ptr, size_t bytes);
+int vkcu_h2d(void *stream, void *dst, const void *src, size_t bytes);
+int vkcu_d2h(void *stream, void *dst, const void *src, size_t bytes);
+int vkcu_d2d(void *stream, void *dst, const void *src, size_t bytes);
+int vkcu_sync(void *stream);
+int vkcu_host_alloc(void **ptr, size_t bytes);
+int vkcu_host_free(void *ptr);
+const char *vkcu_error_string(int code);
+uint64_t vkcu_launch_count(void);
+void vkcu_count_launches(uint64_t n);
+int vkcu_capture_begin(void *stream);
+int vkcu_capture_end(void *stream, void **exec);
+int vkcu_graph_launch(void *exec, void *stream);
+int vkcu_graph_destroy(void *exec);
+
+/* ---- element-wise kernels (elem.cu); `len` elements of `res` ---- */
+int vkcu_elemmul(void *stream, uint64_t *res, const uint64_t *a,
+		const uint64_t *b, uint64_t len, uint64_t mod, uint64_t mu, uint32_t bits);
+int vkcu_elemmulconst(void *stream, uint64_t *res, const uint64_t *a,
+		uint64_t len, uint64_t c, uint64_t c_shoup, uint64_t mod);
+int vkcu_elemfma(void *stream, uint64_t *res, const uint64_t *a,
+		const uint64_t *b, uint64_t len, uint64_t m, uint64_t m_shoup,
+		uint64_t mod);
+int vkcu_elemfma_canonical(void *stream, uint64_t *res, const uint64_t *a,
+		const uint64_t *b, uint64_t len, uint64_t m_red, uint64_t m_shoup,
+		uint64_t mod, uint64_t mu, uint32_t bits);
+int vkcu_elemgtsub(void *stream, uint64_t *res, const uint64_t *a,
+		uint64_t len, uint64_t bound, uint64_t diff_red, uint64_t mod,
+		uint64_t mu, uint32_t bits);
+int vkcu_elemgtadd(void *stream, uint64_t *res, const uint64_t *a,
+		uint64_t len, uint64_t bound, uint64_t diff);
+int vkcu_elemmodbytwo(void *stream, uint64_t *res, const uint64_t *a,
+		uint64_t len, uint64_t signed_bound);
+
+/* ---- transforms (ntt.cu) ----
+ * `jobs` is a device array of `njobs` jobs that all share log_n, or NULL to
+ * launch the single job `one` passed by value.  `scratch` (large n only)
+ * holds njobs * n words when the transform is done in several passes. */
+int vkcu_ntt_forward(void *stream, const vkcu_ntt_job *jobs, int njobs,
+		const vkcu_ntt_job *one, uint32_t log_n, int sms);
+int vkcu_ntt_inverse(void *stream, const vkcu_ntt_job *jobs, int njobs,
+		const vkcu_ntt_job *one, uint32_t log_n, int sms);
+int vkcu_polymul(void *stream, const vkcu_poly_job *jobs, int njobs,
+		const vkcu_poly_job *one, uint32_t log_n, int sms);
+/* c = c * scratch mod q (lazy inputs from the forward transforms, canonical
+ * output) for every job: the pointwise step of a polymul that is not fused. */
+int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,
+		uint32_t log_n, int sms);
+/* Largest log_n the fused single-launch kernels handle. */
+uint32_t vkcu_max_fused_log_n(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
