@@ -47,6 +47,12 @@ int vkhel_ctx_sm_count(const struct vkhel_ctx *ctx);
 /* Kernels launched by this library in this process (graph replays count
  * each kernel node once per replay). */
 uint64_t vkhel_launch_count(void);
+/* Integer-pipe peak of the context's GPU, measured now: independent lazy
+ * Cooley-Tukey butterflies per second with all operands in registers (the
+ * roofline denominator of the transform kernels) and 32-bit IMADs per
+ * second.  Allocates and frees a few KB of device memory. */
+int vkhel_measure_int_peak(struct vkhel_ctx *ctx, double *butterflies_per_s,
+		double *imad_per_s);
 
 /* ---- vectors ---- */
 uint64_t vkhel_vector_length(const struct vkhel_vector *v);

@@ -15,6 +15,7 @@ turns into assert() aborts raise VkhelError here, carrying the library's
 status code and message.  There is no fallback: if the library is missing,
 importing ``lib()`` raises.
 """
+import atexit
 import ctypes
 import os
 import weakref
@@ -58,6 +59,7 @@ _SIGNATURES = [
     ("vkhel_ctx_sync", ctypes.c_int, [vp]),
     ("vkhel_ctx_sm_count", ctypes.c_int, [vp]),
     ("vkhel_launch_count", u64, []),
+    ("vkhel_measure_int_peak", ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("vkhel_vector_length", u64, [vp]),
     ("vkhel_vector_device_ptr", vp, [vp]),
     ("vkhel_vector_upload", ctypes.c_int, [vp, vp, u64]),
@@ -83,6 +85,18 @@ STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "BUDGET", 4: "D
 BATCH_GRAPH = 1
 
 _lib = None
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all_contexts():
+    # Destroy contexts (and their vectors) while the interpreter and the CUDA
+    # runtime are fully alive, instead of in arbitrary finalizer order.
+    for c in list(_live_contexts):
+        try:
+            c.close()
+        except Exception:
+            pass
 
 
 class VkhelError(RuntimeError):
@@ -145,6 +159,7 @@ class Context:
             code, msg = last_error(None)
             raise VkhelError(code or 5, msg)
         self._children = weakref.WeakSet()
+        _live_contexts.add(self)
 
     def close(self):
         if self.ptr:
@@ -185,6 +200,12 @@ class Context:
 
     def vector(self, length_or_data, zero=True):
         return Vector(self, length_or_data, zero)
+
+    def measure_int_peak(self):
+        """(butterflies/s, IMAD/s) of this GPU, measured now."""
+        b, i = ctypes.c_double(), ctypes.c_double()
+        _status(self.ptr, lib().vkhel_measure_int_peak(self.ptr, ctypes.byref(b), ctypes.byref(i)))
+        return b.value, i.value
 
 
 class NttTables:
@@ -246,9 +267,10 @@ class Vector:
         return v
 
     def close(self):
-        if getattr(self, "ptr", None):
+        # A vector outliving its context was freed with the context's pool.
+        if getattr(self, "ptr", None) and getattr(self.ctx, "ptr", None):
             lib().vkhel_vector_destroy(self.ptr)
-            self.ptr = None
+        self.ptr = None
 
     def __del__(self):
         try:
@@ -358,9 +380,9 @@ class Batch:
         return lib().vkhel_batch_kernels(self.ptr)
 
     def close(self):
-        if getattr(self, "ptr", None):
+        if getattr(self, "ptr", None) and getattr(self.ctx, "ptr", None):
             lib().vkhel_batch_destroy(self.ptr)
-            self.ptr = None
+        self.ptr = None
 
     def __del__(self):
         try:

@@ -143,6 +143,12 @@ void *vkhel_ctx_stream(struct vkhel_ctx *ctx) { return ctx ? ctx->stream : NULL;
 int vkhel_ctx_sm_count(const struct vkhel_ctx *ctx) { return ctx ? ctx->sms : 0; }
 uint64_t vkhel_launch_count(void) { return vkcu_launch_count(); }
 
+int vkhel_measure_int_peak(struct vkhel_ctx *ctx, double *bfly, double *imad) {
+	if (!ctx || !bfly || !imad)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "measure_int_peak: NULL argument");
+	return vkh_cuda(ctx, vkcu_measure_int_peak(ctx->stream, ctx->sms, bfly, imad), "measure_int_peak");
+}
+
 int vkhel_ctx_sync(struct vkhel_ctx *ctx) {
 	if (!ctx)
 		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "sync: NULL context");

@@ -47,11 +47,15 @@ struct OpFmaRef {
 };
 
 // (a m + b) mod q for any 64-bit a, b; m is given reduced with its Shoup factor.
+// A Shoup product is exact only while 2q fits in 64 bits; moduli of 2^63 and
+// above take an exact 128-bit remainder instead.
 struct OpFmaCanon {
   u64 m, ms, mod, mu;
   u32 bits;
   __device__ __forceinline__ u64 operator()(u64 a, u64 b) const {
-    const u64 p = shoup(ref_reduce64(a, mod, mu, bits), m, ms, mod);
+    const u64 x = ref_reduce64(a, mod, mu, bits);
+    const u64 p = bits < 64 ? shoup(x, m, ms, mod)
+                            : (u64)(((unsigned __int128)x * m) % mod);
     const u64 y = ref_reduce64(b, mod, mu, bits);
     const u64 s = p + y;
     return (s < p || s >= mod) ? s - mod : s;

@@ -102,6 +102,8 @@ int vkcu_polymul(void *stream, const vkcu_poly_job *jobs, int njobs,
  * output) for every job: the pointwise step of a polymul that is not fused. */
 int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,
 		uint32_t log_n, int sms);
+/* Integer-pipe microbenchmarks (peak.cu). */
+int vkcu_measure_int_peak(void *stream, int sms, double *bfly_per_s, double *imad_per_s);
 /* Largest log_n the fused single-launch kernels handle. */
 uint32_t vkcu_max_fused_log_n(void);
 
