@@ -1,0 +1,524 @@
+// Shared device code of the negacyclic NTT / INTT / fused polymul kernels.
+//
+// Transform convention (identical to the reference):
+//   forward  = the Cooley-Tukey stage loop of src/vector.c:536-566 with the
+//              butterfly of src/kernels/shaders/nttfwdbutterfly.comp:41-57,
+//              natural order in, bit-reversed order out;
+//   inverse  = the Gentleman-Sande loop of src/vector.c:599-630 with the
+//              butterfly of nttrevbutterfly.comp:41-57, bit-reversed in,
+//              natural out, then x n^-1 (src/vector.c:632-638);
+//   twiddles = powers of w in bit-reversed order, root index m + block
+//              (src/ntt_tables.c:25-43, src/kernels/nttfwdbutterfly.c:154-159).
+//
+// GB300 design.  One CTA owns one polynomial of n = 2^LOGN <= 2^14 words
+// held in shared memory (padded by one word per 16: index a -> a + a/16,
+// which makes every access pattern below free of bank conflicts).  The
+// log2(n) butterfly stages run as passes of up to 4 stages: in a pass every
+// thread loads radix-2^k groups of words into registers, one group at a time,
+// runs the k stages on them and writes them back, so at most 16 words (plus
+// their twiddles) are live per thread.  Exceptions:
+//   * the first forward pass reads all of the thread's words from global
+//     memory up front (the loads are coalesced and all in flight at once);
+//   * the last forward pass works on groups of 16 consecutive words, whose
+//     results leave with 32-byte vector stores, or -- in the fused polymul --
+//     are multiplied pointwise by NTT(b) and run through the first inverse
+//     pass in the same registers;
+//   * the last inverse pass folds n^-1 into its final stage and writes global
+//     memory coalesced.
+// Butterflies are lazy (Harvey): values stay in [0, 4q) (forward) or [0, 2q)
+// (inverse) and are made canonical once at the end.
+//
+// Bit-exactness for unreduced inputs.  The reference's first stage computes
+// (X + WY) mod 2^64 mod q and (X - WY) mod q (forward), or (X + Y) mod 2^64
+// mod q and W (X - Y mod q) (inverse).  All later stages see canonical values,
+// so only the first stage needs the reference's wrap-around behaviour; it is
+// taken on a rarely-used branch whenever an input is >= 2q.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "arith.cuh"
+#include "kernels.h"
+
+namespace vk {
+
+template <int I, int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (I < N) {
+    f(std::integral_constant<int, I>{});
+    static_for<I + 1, N>(f);
+  }
+}
+
+__device__ __forceinline__ int pad(int a) { return a + (a >> 4); }
+
+__device__ __forceinline__ ulonglong2 ld_tw(const ulonglong2* p) {
+  ulonglong2 r;
+  asm("ld.global.nc.v2.u64 {%0,%1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ u64 ld_stream(const u64* p) {
+  u64 r;
+  asm volatile("ld.global.L1::no_allocate.u64 %0, [%1];" : "=l"(r) : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ void ld4(const u64* p, u64& a, u64& b, u64& c, u64& d) {
+  asm volatile("ld.global.v4.u64 {%0,%1,%2,%3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(d) : "l"(p));
+}
+
+__device__ __forceinline__ void st4(u64* p, u64 a, u64 b, u64 c, u64 d) {
+  asm volatile("st.global.v4.u64 [%0], {%1,%2,%3,%4};" ::"l"(p), "l"(a), "l"(b), "l"(c), "l"(d) : "memory");
+}
+
+// Bring `bytes` at p into L2 ahead of use (no registers, no completion wait).
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Per-transform constants, loaded once per job into registers.
+struct Tw {
+  u64 q, q2, mu, ninv, ninv_s, w1ninv, w1ninv_s;
+  u32 qbits;
+  const ulonglong2* fwd;
+  const ulonglong2* inv;
+};
+
+__device__ __forceinline__ Tw load_tw(const vkcu_twset* p) {
+  Tw t;
+  t.q = __ldg(reinterpret_cast<const u64*>(&p->q));
+  t.q2 = __ldg(reinterpret_cast<const u64*>(&p->q2));
+  t.mu = __ldg(reinterpret_cast<const u64*>(&p->mu));
+  t.ninv = __ldg(reinterpret_cast<const u64*>(&p->ninv));
+  t.ninv_s = __ldg(reinterpret_cast<const u64*>(&p->ninv_s));
+  t.w1ninv = __ldg(reinterpret_cast<const u64*>(&p->w1ninv));
+  t.w1ninv_s = __ldg(reinterpret_cast<const u64*>(&p->w1ninv_s));
+  t.qbits = __ldg(&p->qbits);
+  t.fwd = reinterpret_cast<const ulonglong2*>(__ldg(reinterpret_cast<const u64*>(&p->fwd)));
+  t.inv = reinterpret_cast<const ulonglong2*>(__ldg(reinterpret_cast<const u64*>(&p->inv)));
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// First-stage butterflies with the reference's exact semantics.
+
+// Forward, stage m = 1.  Fast path whenever x < 2q: then x + WY < 3q < 2^64,
+// so the reference does not wrap and the lazy result is congruent.
+__device__ __forceinline__ void ct_first(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
+  if (x < t.q2) {
+    ct_bfly(x, y, w, wp, t.q, t.q2);
+  } else {
+    const u64 wy = shoup(y, w, wp, t.q);
+    const u64 xr = ref_reduce64(x, t.q, t.mu, t.qbits);
+    const u64 s = ref_reduce64(x + wy, t.q, t.mu, t.qbits);
+    y = xr >= wy ? xr - wy : xr + t.q - wy;
+    x = s;
+  }
+}
+
+// Inverse, stage m = n/2: the sum s and difference d before the twiddle
+// product; s in [0, 4q), d in (0, 4q).
+__device__ __forceinline__ void gs_first_sd(u64 x, u64 y, const Tw& t, u64& s, u64& d) {
+  if (x < t.q2 && y < t.q2) {
+    s = x + y;
+    d = x - y + t.q2;
+  } else {
+    s = ref_reduce64(x + y, t.q, t.mu, t.qbits);
+    const u64 xr = ref_reduce64(x, t.q, t.mu, t.qbits);
+    const u64 yr = ref_reduce64(y, t.q, t.mu, t.qbits);
+    d = xr >= yr ? xr - yr : xr + t.q - yr;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Register-resident radix-2^KK groups.  A group holds 2^KK words v[G0 + j]
+// at stride t_min of the transform, all inside one block of the first stage
+// of the pass; `base` = (tw_mult * m0 + block) so that the root of sub-stage u
+// and sub-block r is table[(base << u) + r].
+
+template <int KK, int U0, int G0, int NV>
+__device__ __forceinline__ void ct_group(u64 (&v)[NV], const ulonglong2* tw, u32 base, const Tw& t) {
+  static_for<U0, KK>([&](auto uc) {
+    constexpr int u = decltype(uc)::value;
+    constexpr int half = 1 << (KK - 1 - u);
+    static_for<0, (1 << u)>([&](auto rc) {
+      constexpr int r = decltype(rc)::value;
+      const ulonglong2 w = ld_tw(tw + ((base << u) + r));
+#pragma unroll
+      for (int jj = 0; jj < half; jj++)
+        ct_bfly(v[G0 + r * 2 * half + jj], v[G0 + r * 2 * half + jj + half], w.x, w.y, t.q, t.q2);
+    });
+  });
+}
+
+// Forward sub-stage 0 of a group with the exact first-stage rule (root index 1).
+template <int KK, int G0, int NV>
+__device__ __forceinline__ void ct_group_first_exact(u64 (&v)[NV], const Tw& t) {
+  constexpr int half = 1 << (KK - 1);
+  const ulonglong2 w = ld_tw(t.fwd + 1);
+#pragma unroll
+  for (int jj = 0; jj < half; jj++) ct_first(v[G0 + jj], v[G0 + jj + half], w.x, w.y, t);
+}
+
+// Inverse group: sub-stages KK-1 .. 0.  EXACT_TOP applies the exact rule to
+// sub-stage KK-1 (global stage m = n/2); FOLD folds n^-1 into sub-stage 0
+// (global stage m = 1, root index 1) and leaves canonical outputs.
+template <int KK, int G0, bool EXACT_TOP, bool FOLD, int NV>
+__device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32 base, const Tw& t) {
+  static_for<0, KK>([&](auto uc) {
+    constexpr int u = KK - 1 - decltype(uc)::value;
+    constexpr int half = 1 << (KK - 1 - u);
+    if constexpr (FOLD && u == 0) {
+#pragma unroll
+      for (int jj = 0; jj < half; jj++) {
+        u64& x = v[G0 + jj];
+        u64& y = v[G0 + jj + half];
+        u64 s, d;
+        if constexpr (EXACT_TOP && u == KK - 1) {
+          gs_first_sd(x, y, t, s, d);
+        } else {
+          s = x + y;
+          d = x - y + t.q2;
+        }
+        x = shoup(s, t.ninv, t.ninv_s, t.q);
+        y = shoup(d, t.w1ninv, t.w1ninv_s, t.q);
+      }
+    } else {
+      static_for<0, (1 << u)>([&](auto rc) {
+        constexpr int r = decltype(rc)::value;
+        const ulonglong2 w = ld_tw(tw + ((base << u) + r));
+#pragma unroll
+        for (int jj = 0; jj < half; jj++) {
+          u64& x = v[G0 + r * 2 * half + jj];
+          u64& y = v[G0 + r * 2 * half + jj + half];
+          if constexpr (EXACT_TOP && u == KK - 1) {
+            u64 s, d;
+            gs_first_sd(x, y, t, s, d);
+            x = csub(s, t.q2);
+            y = shoup_lazy(d, w.x, w.y, t.q);
+          } else {
+            gs_bfly(x, y, w.x, w.y, t.q, t.q2);
+          }
+        }
+      });
+    }
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Pass schedule for n = 2^LOGN held by T = n/E threads.  Passes have at most
+// 4 stages; the last has exactly 4 (groups of 16 consecutive words) and the
+// first takes the remainder, so every head pass has t_min >= 16.
+
+template <int LOGN_, int E_>
+struct Shape {
+  static constexpr int LOGN = LOGN_, E = E_;
+  static constexpr int N = 1 << LOGN, T = N / E;
+  static constexpr int K = 4;
+  static constexpr int HEAD = LOGN - 4;  // stages before the last pass
+  static constexpr int NHEAD = (HEAD + K - 1) / K;
+  static constexpr int FIRSTK = HEAD - K * (NHEAD - 1);
+  static constexpr int SMEM_BYTES = (N + N / 16) * 8;
+  static_assert(E >= 16 && (E % 16) == 0 && HEAD >= 1 && T >= 1, "unsupported shape");
+  template <int P>
+  static constexpr int s0() { return P == 0 ? 0 : FIRSTK + K * (P - 1); }
+  template <int P>
+  static constexpr int kk() { return P == 0 ? FIRSTK : K; }
+};
+
+// Group i of this thread in a pass starting at stage S0 with KK stages:
+// g = tid + i*T, block b = g / TMIN, first word b*(n >> S0) + g % TMIN,
+// word j at + j*TMIN.
+template <class S, int S0, int KK>
+struct PassMap {
+  static constexpr int G = S::E >> KK, TMIN = S::N >> (S0 + KK), BLK = S::N >> S0;
+  __device__ __forceinline__ static int g(int i) { return (int)threadIdx.x + i * S::T; }
+  __device__ __forceinline__ static int first(int i) { return (g(i) / TMIN) * BLK + (g(i) % TMIN); }
+  __device__ __forceinline__ static u32 base(u32 tw_mult, int i) { return tw_mult * (1u << S0) + (u32)(g(i) / TMIN); }
+};
+
+// Forward head pass P >= 1: shared -> registers -> shared, group by group.
+template <class S, int P>
+__device__ __forceinline__ void fwd_pass_smem(u64* sm, const Tw& t, u32 tw_mult) {
+  constexpr int S0 = S::template s0<P>(), KK = S::template kk<P>();
+  using M = PassMap<S, S0, KK>;
+#pragma unroll 1
+  for (int i = 0; i < M::G; i++) {
+    const int a0 = M::first(i);
+    u64 v[1 << KK];
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(a0 + j * M::TMIN)];
+    ct_group<KK, 0, 0>(v, t.fwd, M::base(tw_mult, i), t);
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) sm[pad(a0 + j * M::TMIN)] = v[j];
+  }
+}
+
+// Inverse head pass P: shared -> registers -> shared (FOLD/out: see inv_ntt).
+template <class S, int P, bool FOLD>
+__device__ __forceinline__ void inv_pass(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out) {
+  constexpr int S0 = S::template s0<P>(), KK = S::template kk<P>();
+  using M = PassMap<S, S0, KK>;
+#pragma unroll 1
+  for (int i = 0; i < M::G; i++) {
+    const int a0 = M::first(i);
+    u64 v[1 << KK];
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(a0 + j * M::TMIN)];
+    gs_group<KK, 0, false, FOLD && P == 0>(v, t.inv, M::base(tw_mult, i), t);
+    if constexpr (P == 0) {
+#pragma unroll
+      for (int j = 0; j < (1 << KK); j++) out[a0 + j * M::TMIN] = v[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < (1 << KK); j++) sm[pad(a0 + j * M::TMIN)] = v[j];
+    }
+  }
+}
+
+// Forward transform of the n words at `in` up to (not including) the last
+// pass; the result is in shared memory, lazy [0, 4q).  EXACT: `in` is caller
+// data and pass 0 starts at global stage 0.
+template <class S, bool EXACT>
+__device__ __forceinline__ void fwd_head(u64* sm, const u64* __restrict__ in, const Tw& t, u32 tw_mult) {
+  {
+    constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+    u64 v[S::E];
+#pragma unroll
+    for (int i = 0; i < G; i++)
+#pragma unroll
+      for (int j = 0; j < (1 << KK); j++)
+        v[i * (1 << KK) + j] = ld_stream(in + (int)threadIdx.x + i * S::T + j * TMIN);
+    static_for<0, G>([&](auto ic) {
+      constexpr int i = decltype(ic)::value;
+      if constexpr (EXACT) {
+        ct_group_first_exact<KK, i * (1 << KK)>(v, t);
+        ct_group<KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
+      } else {
+        ct_group<KK, 0, i * (1 << KK)>(v, t.fwd, tw_mult, t);
+      }
+      const int g = (int)threadIdx.x + i * S::T;
+#pragma unroll
+      for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
+    });
+  }
+  __syncthreads();
+  static_for<1, S::NHEAD>([&](auto pc) {
+    fwd_pass_smem<S, decltype(pc)::value>(sm, t, tw_mult);
+    __syncthreads();
+  });
+}
+
+// Last forward pass: for each group of 16 consecutive words (g = tid + i*T,
+// words 16g .. 16g+15) load from shared memory, run the 4 stages, hand the
+// registers to `epi(g, v)`.
+template <class S, class Epi>
+__device__ __forceinline__ void fwd_last(u64* sm, const Tw& t, u32 tw_mult, Epi&& epi) {
+#pragma unroll 1
+  for (int i = 0; i < S::E / 16; i++) {
+    const int g = (int)threadIdx.x + i * S::T;
+    u64 v[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = sm[pad(16 * g + j)];
+    ct_group<4, 0, 0>(v, t.fwd, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+    epi(g, v);
+  }
+}
+
+// Inverse transform from the first-pass layout: `first(g, v)` fills and runs
+// the first inverse pass for group g (16 consecutive words) and the result is
+// stored to shared memory; the remaining passes follow; the last writes `out`.
+// FOLD: whole transform (tw_mult == 1), n^-1 folded in, canonical output;
+// otherwise lazy [0, 2q).
+template <class S, bool FOLD, class First>
+__device__ __forceinline__ void inv_ntt(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, First&& first) {
+#pragma unroll 1
+  for (int i = 0; i < S::E / 16; i++) {
+    const int g = (int)threadIdx.x + i * S::T;
+    u64 v[16];
+    first(g, v);
+#pragma unroll
+    for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
+  }
+  __syncthreads();
+  static_for<0, S::NHEAD>([&](auto pc) {
+    constexpr int P = S::NHEAD - 1 - decltype(pc)::value;  // NHEAD-1 .. 0
+    inv_pass<S, P, FOLD>(sm, t, tw_mult, out);
+    if constexpr (P > 0) __syncthreads();
+  });
+}
+
+// Register groups of 16 consecutive words <-> global memory (32-byte vectors).
+__device__ __forceinline__ void load16(u64 (&v)[16], const u64* p) {
+#pragma unroll
+  for (int h = 0; h < 4; h++) ld4(p + 4 * h, v[4 * h], v[4 * h + 1], v[4 * h + 2], v[4 * h + 3]);
+}
+
+__device__ __forceinline__ void store16(const u64 (&v)[16], u64* p) {
+#pragma unroll
+  for (int h = 0; h < 4; h++) st4(p + 4 * h, v[4 * h], v[4 * h + 1], v[4 * h + 2], v[4 * h + 3]);
+}
+
+// Resident CTAs per SM the register budget is sized for: 512 threads per SM
+// (128 registers per thread) for the 32-words-per-thread shapes, 384 threads
+// (about 170 registers) for the 16-words-per-thread shapes, whose fused
+// pointwise step holds two 16-word groups.
+template <int LOGN, int E>
+constexpr int min_blocks() {
+  constexpr int budget = E >= 32 ? 512 : 384;
+  return (budget / ((1 << LOGN) / E)) < 1 ? 1 : (budget / ((1 << LOGN) / E));
+}
+
+template <class J>
+__device__ __forceinline__ J fetch_job(const J* jobs, const J& one, int jid) {
+  return jobs ? jobs[jid] : one;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels.  Jobs come from a device array (persistent loop over
+// blockIdx.x, blockIdx.x + gridDim.x, ...) or, for a single job, by value.
+// sub_log > 0: each job is split into 2^sub_log sub-blocks of 2^LOGN words
+// (transforms of 2^(LOGN + sub_log) words after / before the global passes).
+
+template <int LOGN, int E>
+__global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
+    k_ntt_fwd(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log) {
+  using S = Shape<LOGN, E>;
+  extern __shared__ u64 sm[];
+  const int total = njobs << sub_log;
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    const vkcu_ntt_job job = fetch_job(jobs, one, w >> sub_log);
+    const int sub = w & ((1 << sub_log) - 1);
+    const Tw t = load_tw(job.tw);
+    u64* out = reinterpret_cast<u64*>(job.out) + ((size_t)sub << LOGN);
+    if (sub_log == 0) {
+      fwd_head<S, true>(sm, reinterpret_cast<const u64*>(job.in), t, 1u);
+      fwd_last<S>(sm, t, 1u, [&](int g, u64(&v)[16]) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+        store16(v, out + 16 * g);
+      });
+    } else {
+      const u32 tw_mult = (1u << sub_log) + sub;
+      fwd_head<S, false>(sm, out, t, tw_mult);
+      fwd_last<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+        store16(v, out + 16 * g);
+      });
+    }
+    __syncthreads();
+  }
+}
+
+template <int LOGN, int E>
+__global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
+    k_ntt_inv(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log) {
+  using S = Shape<LOGN, E>;
+  extern __shared__ u64 sm[];
+  const int total = njobs << sub_log;
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    const vkcu_ntt_job job = fetch_job(jobs, one, w >> sub_log);
+    const int sub = w & ((1 << sub_log) - 1);
+    const Tw t = load_tw(job.tw);
+    const u64* in = reinterpret_cast<const u64*>(job.in) + ((size_t)sub << LOGN);
+    u64* out = reinterpret_cast<u64*>(job.out) + ((size_t)sub << LOGN);
+    const u32 tw_mult = (1u << sub_log) + sub;
+    auto first = [&](int g, u64(&v)[16]) {
+      load16(v, in + 16 * g);
+      gs_group<4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+    };
+    if (sub_log == 0)
+      inv_ntt<S, true>(sm, t, 1u, out, first);
+    else
+      inv_ntt<S, false>(sm, t, tw_mult, out, first);
+    __syncthreads();
+  }
+}
+
+// Fused c = INTT(NTT(a) . NTT(b)).  NTT(b) goes to job.scratch (canonical);
+// NTT(a)'s last pass, the pointwise product (NTT(b) read back at the words
+// this thread wrote) and the first inverse pass share registers, group by
+// group; the inverse writes c.  a is prefetched into L2 while NTT(b) runs.
+template <int LOGN, int E>
+__global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
+    k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one) {
+  using S = Shape<LOGN, E>;
+  extern __shared__ u64 sm[];
+  for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
+    const vkcu_poly_job job = fetch_job(jobs, one, w);
+    const Tw t = load_tw(job.tw);
+    u64* scratch = reinterpret_cast<u64*>(job.scratch);
+    if (threadIdx.x < 4) {
+      constexpr unsigned chunk = (unsigned)(S::N * 8 / 4);
+      prefetch_l2(reinterpret_cast<const char*>(job.a) + threadIdx.x * chunk, chunk);
+    }
+    fwd_head<S, true>(sm, reinterpret_cast<const u64*>(job.b), t, 1u);
+    fwd_last<S>(sm, t, 1u, [&](int g, u64(&v)[16]) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+      store16(v, scratch + 16 * g);
+    });
+    __syncthreads();
+    fwd_head<S, true>(sm, reinterpret_cast<const u64*>(job.a), t, 1u);
+    if (w + (int)gridDim.x < njobs && threadIdx.x < 4) {
+      const vkcu_poly_job nx = fetch_job(jobs, one, w + (int)gridDim.x);
+      constexpr unsigned chunk = (unsigned)(S::N * 8 / 4);
+      prefetch_l2(reinterpret_cast<const char*>(nx.b) + threadIdx.x * chunk, chunk);
+    }
+    // The first inverse pass reads its words from registers and writes them
+    // to the same shared-memory slots the last forward pass read them from.
+    inv_ntt<S, true>(sm, t, 1u, reinterpret_cast<u64*>(job.c), [&](int g, u64(&v)[16]) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] = sm[pad(16 * g + j)];
+      ct_group<4, 0, 0>(v, t.fwd, (u32)(S::N / 16) + (u32)g, t);
+      u64 bh[16];
+      load16(bh, scratch + 16 * g);
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+      gs_group<4, 0, false, false>(v, t.inv, (u32)(S::N / 16) + (u32)g, t);
+    });
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: per-family launchers (one translation unit each).
+
+int fwd_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log,
+            int sms);
+int inv_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log,
+            int sms);
+int poly_cta(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms);
+
+template <class K>
+static int prepare(K kernel, int smem) {
+  return (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+template <class K>
+static int grid_for(K kernel, int threads, int smem, long work, int sms) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const long cap = (long)per_sm * (sms > 0 ? sms : 1);
+  return (int)(work < cap ? work : cap);
+}
+
+// Elements per thread for each fused degree.
+#define VK_FOR_LOGN(X)                          \
+  switch (log_n) {                              \
+    case 8: return X(8, 16);                    \
+    case 9: return X(9, 16);                    \
+    case 10: return X(10, 16);                  \
+    case 11: return X(11, 16);                  \
+    case 12: return X(12, 16);                  \
+    case 13: return X(13, 32);                  \
+    case 14: return X(14, 32);                  \
+    default: return (int)cudaErrorInvalidValue; \
+  }
+
+}  // namespace vk

@@ -1,0 +1,26 @@
+// Launcher of the CTA-resident forward transforms for 2^8 <= n <= 2^14 (kernel in
+// ntt_core.cuh); one translation unit per kernel family so they compile in
+// parallel.
+#include "ntt_core.cuh"
+
+namespace vk {
+
+template <int LOGN, int E>
+static int launch(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int sub_log, int sms) {
+  using S = Shape<LOGN, E>;
+  auto kern = k_ntt_fwd<LOGN, E>;
+  static const int prepared = prepare(kern, S::SMEM_BYTES);
+  if (prepared) return prepared;
+  const int grid = grid_for(kern, S::T, S::SMEM_BYTES, (long)njobs << sub_log, sms);
+  kern<<<grid, S::T, S::SMEM_BYTES, st>>>(jobs, njobs, one, sub_log);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+int fwd_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log, int sms) {
+#define X(L, E) launch<L, E>(st, jobs, njobs, one, sub_log, sms)
+  VK_FOR_LOGN(X)
+#undef X
+}
+
+}  // namespace vk
