@@ -62,6 +62,11 @@ uint64_t *vkhel_vector_device_ptr(struct vkhel_vector *v);
  * the vector (count <= length). */
 int vkhel_vector_upload(struct vkhel_vector *v, const uint64_t *src, uint64_t count);
 int vkhel_vector_download(const struct vkhel_vector *v, uint64_t *dst, uint64_t count);
+/* Stream-ordered variants: enqueue the copy on the context stream and return.
+ * The host buffer must stay valid (and should be pinned for the copy to be
+ * truly asynchronous) until vkhel_ctx_sync returns. */
+int vkhel_vector_upload_async(struct vkhel_vector *v, const uint64_t *src, uint64_t count);
+int vkhel_vector_download_async(const struct vkhel_vector *v, uint64_t *dst, uint64_t count);
 /* Print the vector (reference: src/vector.c:237-247, exported there through
  * the vkhel_* glob of vkhel.syms). */
 void vkhel_vector_dbgprint(const struct vkhel_vector *v);

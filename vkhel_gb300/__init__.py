@@ -64,6 +64,8 @@ _SIGNATURES = [
     ("vkhel_vector_device_ptr", vp, [vp]),
     ("vkhel_vector_upload", ctypes.c_int, [vp, vp, u64]),
     ("vkhel_vector_download", ctypes.c_int, [vp, vp, u64]),
+    ("vkhel_vector_upload_async", ctypes.c_int, [vp, vp, u64]),
+    ("vkhel_vector_download_async", ctypes.c_int, [vp, vp, u64]),
     ("vkhel_vector_dbgprint", None, [vp]),
     ("vkhel_ntt_tables_copy", ctypes.c_int, [vp, vp, vp, vp, vp]),
     ("vkhel_ntt_tables_dbgprint", None, [vp]),

@@ -253,6 +253,18 @@ int vkhel_vector_download(const struct vkhel_vector *v, uint64_t *dst, uint64_t 
 	return vkh_cuda(v->ctx, e, "download");
 }
 
+int vkhel_vector_upload_async(struct vkhel_vector *v, const uint64_t *src, uint64_t count) {
+	if (!v || (!src && count) || count > v->length)
+		return vkh_fail(v ? v->ctx : NULL, VKHEL_ERR_INVALID_ARGUMENT, "upload_async: bad argument");
+	return vkh_cuda(v->ctx, vkcu_h2d(v->ctx->stream, v->dev, src, count * sizeof(uint64_t)), "upload_async");
+}
+
+int vkhel_vector_download_async(const struct vkhel_vector *v, uint64_t *dst, uint64_t count) {
+	if (!v || (!dst && count) || count > v->length)
+		return vkh_fail(v ? v->ctx : NULL, VKHEL_ERR_INVALID_ARGUMENT, "download_async: bad argument");
+	return vkh_cuda(v->ctx, vkcu_d2h(v->ctx->stream, dst, v->dev, count * sizeof(uint64_t)), "download_async");
+}
+
 /* Reference: map + memcpy + unmap (src/vector.c:262-268); one direct copy here. */
 void vkhel_vector_copy_from_host(struct vkhel_vector *v, const uint64_t *e) {
 	if (!v)

@@ -83,7 +83,7 @@ __global__ void k_ntt_inv_simple(const vkcu_ntt_job* __restrict__ jobs, int njob
 
 // ---------------------------------------------------------------------------
 // Global-memory passes for n > 2^14 (KK = log2(n) - 14 stages, KK <= 4).
-// Forward: global stages 0 .. KK-1, in -> out, lazy [0, 4q).  Each thread
+// Forward: global stages 0 .. KK-1, in -> out, lazy [0, 2q).  Each thread
 // owns one group of 2^KK words at stride n / 2^KK (coalesced).
 template <int KK>
 __global__ void k_fwd_head_global(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
@@ -98,11 +98,14 @@ __global__ void k_fwd_head_global(const vkcu_ntt_job* __restrict__ jobs, int njo
     u64 v[1 << KK];
 #pragma unroll
     for (int j = 0; j < (1 << KK); j++) v[j] = ld_stream(in + o + (size_t)j * groups);
-    ct_group_first_exact<KK, 0>(v, t);
+    const ulonglong2 w0 = ld_tw(t.fwd + 1);
+#pragma unroll
+    for (int jj = 0; jj < (1 << (KK - 1)); jj++) ct_first(v[jj], v[jj + (1 << (KK - 1))], w0.x, w0.y, t);
     ct_group<KK, 1, 0>(v, t.fwd, 1u, t);
     u64* out = reinterpret_cast<u64*>(job.out);
+    // below 2q, so the sub-block kernels' first stage stays on its fast path
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) out[o + (size_t)j * groups] = v[j];
+    for (int j = 0; j < (1 << KK); j++) out[o + (size_t)j * groups] = csub(v[j], t.q2);
   }
 }
 

@@ -105,31 +105,46 @@ __device__ __forceinline__ Tw load_tw(const vkcu_twset* p) {
 // ---------------------------------------------------------------------------
 // First-stage butterflies with the reference's exact semantics.
 
+struct U2 {
+  u64 x, y;
+};
+
+// The reference's stage-0 butterfly for x >= 2q, exactly: X' = (X + WY) mod
+// 2^64 mod q, Y' = (X - WY) mod q.  Kept out of line: it is rarely taken.
+static __device__ __noinline__ U2 ct_first_slow(u64 x, u64 y, u64 w, u64 wp, u64 q, u64 mu, u32 qbits) {
+  const u64 wy = shoup(y, w, wp, q);
+  const u64 xr = ref_reduce64(x, q, mu, qbits);
+  return U2{ref_reduce64(x + wy, q, mu, qbits), xr >= wy ? xr - wy : xr + q - wy};
+}
+
 // Forward, stage m = 1.  Fast path whenever x < 2q: then x + WY < 3q < 2^64,
 // so the reference does not wrap and the lazy result is congruent.
 __device__ __forceinline__ void ct_first(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
   if (x < t.q2) {
     ct_bfly(x, y, w, wp, t.q, t.q2);
   } else {
-    const u64 wy = shoup(y, w, wp, t.q);
-    const u64 xr = ref_reduce64(x, t.q, t.mu, t.qbits);
-    const u64 s = ref_reduce64(x + wy, t.q, t.mu, t.qbits);
-    y = xr >= wy ? xr - wy : xr + t.q - wy;
-    x = s;
+    const U2 r = ct_first_slow(x, y, w, wp, t.q, t.mu, t.qbits);
+    x = r.x;
+    y = r.y;
   }
 }
 
 // Inverse, stage m = n/2: the sum s and difference d before the twiddle
 // product; s in [0, 4q), d in (0, 4q).
+static __device__ __noinline__ U2 gs_first_slow(u64 x, u64 y, u64 q, u64 mu, u32 qbits) {
+  const u64 xr = ref_reduce64(x, q, mu, qbits);
+  const u64 yr = ref_reduce64(y, q, mu, qbits);
+  return U2{ref_reduce64(x + y, q, mu, qbits), xr >= yr ? xr - yr : xr + q - yr};
+}
+
 __device__ __forceinline__ void gs_first_sd(u64 x, u64 y, const Tw& t, u64& s, u64& d) {
   if (x < t.q2 && y < t.q2) {
     s = x + y;
     d = x - y + t.q2;
   } else {
-    s = ref_reduce64(x + y, t.q, t.mu, t.qbits);
-    const u64 xr = ref_reduce64(x, t.q, t.mu, t.qbits);
-    const u64 yr = ref_reduce64(y, t.q, t.mu, t.qbits);
-    d = xr >= yr ? xr - yr : xr + t.q - yr;
+    const U2 r = gs_first_slow(x, y, t.q, t.mu, t.qbits);
+    s = r.x;
+    d = r.y;
   }
 }
 
@@ -152,15 +167,6 @@ __device__ __forceinline__ void ct_group(u64 (&v)[NV], const ulonglong2* tw, u32
         ct_bfly(v[G0 + r * 2 * half + jj], v[G0 + r * 2 * half + jj + half], w.x, w.y, t.q, t.q2);
     });
   });
-}
-
-// Forward sub-stage 0 of a group with the exact first-stage rule (root index 1).
-template <int KK, int G0, int NV>
-__device__ __forceinline__ void ct_group_first_exact(u64 (&v)[NV], const Tw& t) {
-  constexpr int half = 1 << (KK - 1);
-  const ulonglong2 w = ld_tw(t.fwd + 1);
-#pragma unroll
-  for (int jj = 0; jj < half; jj++) ct_first(v[G0 + jj], v[G0 + jj + half], w.x, w.y, t);
 }
 
 // Inverse group: sub-stages KK-1 .. 0.  EXACT_TOP applies the exact rule to
@@ -209,146 +215,134 @@ __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32
 }
 
 // ---------------------------------------------------------------------------
-// Pass schedule for n = 2^LOGN held by T = n/E threads.  Passes have at most
-// 4 stages; the last has exactly 4 (groups of 16 consecutive words) and the
-// first takes the remainder, so every head pass has t_min >= 16.
+// Pass schedule for n = 2^LOGN held by T = n/E threads.  The first pass has
+// FIRSTK <= 4 stages and reads global memory; every later pass has exactly 4
+// stages (radix 16) and runs on shared memory; the last one starts at stage
+// HEAD = LOGN - 4 and sees groups of 16 consecutive words.  Every pass but the
+// first has t_min >= 16 or is the last pass.
+//
+// Code size matters as much as instruction count here: all radix-16 passes of
+// a direction share one loop body (the stage offset is a runtime value), and
+// the fused polymul runs its two forward transforms through the same code.
 
 template <int LOGN_, int E_>
 struct Shape {
   static constexpr int LOGN = LOGN_, E = E_;
   static constexpr int N = 1 << LOGN, T = N / E;
-  static constexpr int K = 4;
-  static constexpr int HEAD = LOGN - 4;  // stages before the last pass
-  static constexpr int NHEAD = (HEAD + K - 1) / K;
-  static constexpr int FIRSTK = HEAD - K * (NHEAD - 1);
+  static constexpr int HEAD = LOGN - 4;  // first stage of the last pass
+  static constexpr int FIRSTK = HEAD % 4 == 0 ? 4 : HEAD % 4;
   static constexpr int SMEM_BYTES = (N + N / 16) * 8;
   static_assert(E >= 16 && (E % 16) == 0 && HEAD >= 1 && T >= 1, "unsupported shape");
-  template <int P>
-  static constexpr int s0() { return P == 0 ? 0 : FIRSTK + K * (P - 1); }
-  template <int P>
-  static constexpr int kk() { return P == 0 ? FIRSTK : K; }
 };
 
-// Group i of this thread in a pass starting at stage S0 with KK stages:
-// g = tid + i*T, block b = g / TMIN, first word b*(n >> S0) + g % TMIN,
-// word j at + j*TMIN.
-template <class S, int S0, int KK>
-struct PassMap {
-  static constexpr int G = S::E >> KK, TMIN = S::N >> (S0 + KK), BLK = S::N >> S0;
-  __device__ __forceinline__ static int g(int i) { return (int)threadIdx.x + i * S::T; }
-  __device__ __forceinline__ static int first(int i) { return (g(i) / TMIN) * BLK + (g(i) % TMIN); }
-  __device__ __forceinline__ static u32 base(u32 tw_mult, int i) { return tw_mult * (1u << S0) + (u32)(g(i) / TMIN); }
+// A radix-16 pass starting at stage s0 of an n = 2^logn transform: group g
+// has block g >> lt (lt = log2 t_min), first word (g >> lt) << lb | (g & mask)
+// with lb = log2(n >> s0), words at stride t_min, twiddle base tw0 + block.
+struct Pass16 {
+  int lt, lb;
+  u32 tw0;
+  __device__ __forceinline__ Pass16(int logn, int s0, u32 tw_mult)
+      : lt(logn - s0 - 4), lb(logn - s0), tw0(tw_mult << s0) {}
+  __device__ __forceinline__ int first(int g) const { return ((g >> lt) << lb) | (g & ((1 << lt) - 1)); }
+  __device__ __forceinline__ u32 base(int g) const { return tw0 + (u32)(g >> lt); }
 };
 
-// Forward head pass P >= 1: shared -> registers -> shared, group by group.
-template <class S, int P>
-__device__ __forceinline__ void fwd_pass_smem(u64* sm, const Tw& t, u32 tw_mult) {
-  constexpr int S0 = S::template s0<P>(), KK = S::template kk<P>();
-  using M = PassMap<S, S0, KK>;
-#pragma unroll 1
-  for (int i = 0; i < M::G; i++) {
-    const int a0 = M::first(i);
-    u64 v[1 << KK];
+// First forward pass: all of this thread's words come from global memory at
+// once (coalesced), then FIRSTK stages per group, results to shared memory.
+// The first sub-stage uses the exact first-stage rule; after the global pass
+// of a large transform the inputs are < 2q and always take its fast path.
+template <class S>
+__device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, const Tw& t, u32 tw_mult) {
+  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+  u64 v[S::E];
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(a0 + j * M::TMIN)];
-    ct_group<KK, 0, 0>(v, t.fwd, M::base(tw_mult, i), t);
+  for (int i = 0; i < G; i++)
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) sm[pad(a0 + j * M::TMIN)] = v[j];
-  }
-}
-
-// Inverse head pass P: shared -> registers -> shared (FOLD/out: see inv_ntt).
-template <class S, int P, bool FOLD>
-__device__ __forceinline__ void inv_pass(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out) {
-  constexpr int S0 = S::template s0<P>(), KK = S::template kk<P>();
-  using M = PassMap<S, S0, KK>;
-#pragma unroll 1
-  for (int i = 0; i < M::G; i++) {
-    const int a0 = M::first(i);
-    u64 v[1 << KK];
+    for (int j = 0; j < (1 << KK); j++) v[i * (1 << KK) + j] = ld_stream(in + (int)threadIdx.x + i * S::T + j * TMIN);
+  const ulonglong2 w0 = ld_tw(t.fwd + tw_mult);
+  static_for<0, G>([&](auto ic) {
+    constexpr int i = decltype(ic)::value;
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(a0 + j * M::TMIN)];
-    gs_group<KK, 0, false, FOLD && P == 0>(v, t.inv, M::base(tw_mult, i), t);
-    if constexpr (P == 0) {
+    for (int jj = 0; jj < (1 << (KK - 1)); jj++)
+      ct_first(v[i * (1 << KK) + jj], v[i * (1 << KK) + jj + (1 << (KK - 1))], w0.x, w0.y, t);
+    ct_group<KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
+    const int g = (int)threadIdx.x + i * S::T;
 #pragma unroll
-      for (int j = 0; j < (1 << KK); j++) out[a0 + j * M::TMIN] = v[j];
-    } else {
-#pragma unroll
-      for (int j = 0; j < (1 << KK); j++) sm[pad(a0 + j * M::TMIN)] = v[j];
-    }
-  }
-}
-
-// Forward transform of the n words at `in` up to (not including) the last
-// pass; the result is in shared memory, lazy [0, 4q).  EXACT: `in` is caller
-// data and pass 0 starts at global stage 0.
-template <class S, bool EXACT>
-__device__ __forceinline__ void fwd_head(u64* sm, const u64* __restrict__ in, const Tw& t, u32 tw_mult) {
-  {
-    constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
-    u64 v[S::E];
-#pragma unroll
-    for (int i = 0; i < G; i++)
-#pragma unroll
-      for (int j = 0; j < (1 << KK); j++)
-        v[i * (1 << KK) + j] = ld_stream(in + (int)threadIdx.x + i * S::T + j * TMIN);
-    static_for<0, G>([&](auto ic) {
-      constexpr int i = decltype(ic)::value;
-      if constexpr (EXACT) {
-        ct_group_first_exact<KK, i * (1 << KK)>(v, t);
-        ct_group<KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
-      } else {
-        ct_group<KK, 0, i * (1 << KK)>(v, t.fwd, tw_mult, t);
-      }
-      const int g = (int)threadIdx.x + i * S::T;
-#pragma unroll
-      for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
-    });
-  }
-  __syncthreads();
-  static_for<1, S::NHEAD>([&](auto pc) {
-    fwd_pass_smem<S, decltype(pc)::value>(sm, t, tw_mult);
-    __syncthreads();
+    for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
   });
+  __syncthreads();
 }
 
-// Last forward pass: for each group of 16 consecutive words (g = tid + i*T,
-// words 16g .. 16g+15) load from shared memory, run the 4 stages, hand the
-// registers to `epi(g, v)`.
+// Radix-16 forward passes s0 = FIRSTK, FIRSTK + 4, ..., HEAD on shared
+// memory.  The last pass hands each group (words 16g .. 16g+15) to epi(g, v)
+// instead of storing it back.  Ends with a barrier.
 template <class S, class Epi>
-__device__ __forceinline__ void fwd_last(u64* sm, const Tw& t, u32 tw_mult, Epi&& epi) {
+__device__ __forceinline__ void fwd_passes(u64* sm, const Tw& t, u32 tw_mult, Epi&& epi) {
 #pragma unroll 1
-  for (int i = 0; i < S::E / 16; i++) {
-    const int g = (int)threadIdx.x + i * S::T;
-    u64 v[16];
+  for (int s0 = S::FIRSTK; s0 <= S::HEAD; s0 += 4) {
+    const Pass16 ps(S::LOGN, s0, tw_mult);
+    const int st = 1 << ps.lt;
+#pragma unroll 1
+    for (int i = 0; i < S::E / 16; i++) {
+      const int g = (int)threadIdx.x + i * S::T;
+      const int a0 = ps.first(g);
+      u64 v[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = sm[pad(16 * g + j)];
-    ct_group<4, 0, 0>(v, t.fwd, tw_mult * (u32)(S::N / 16) + (u32)g, t);
-    epi(g, v);
+      for (int j = 0; j < 16; j++) v[j] = sm[pad(a0 + j * st)];
+      ct_group<4, 0, 0>(v, t.fwd, ps.base(g), t);
+      if (s0 < S::HEAD) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) sm[pad(a0 + j * st)] = v[j];
+      } else {
+        epi(g, v);
+      }
+    }
+    __syncthreads();
   }
 }
 
-// Inverse transform from the first-pass layout: `first(g, v)` fills and runs
-// the first inverse pass for group g (16 consecutive words) and the result is
-// stored to shared memory; the remaining passes follow; the last writes `out`.
-// FOLD: whole transform (tw_mult == 1), n^-1 folded in, canonical output;
-// otherwise lazy [0, 2q).
-template <class S, bool FOLD, class First>
-__device__ __forceinline__ void inv_ntt(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, First&& first) {
+// Radix-16 inverse passes s0 = s_top, s_top - 4, ..., FIRSTK on shared
+// memory, each followed by a barrier.
+template <class S>
+__device__ __forceinline__ void inv_passes(u64* sm, const Tw& t, u32 tw_mult, int s_top) {
 #pragma unroll 1
-  for (int i = 0; i < S::E / 16; i++) {
-    const int g = (int)threadIdx.x + i * S::T;
-    u64 v[16];
-    first(g, v);
+  for (int s0 = s_top; s0 >= S::FIRSTK; s0 -= 4) {
+    const Pass16 ps(S::LOGN, s0, tw_mult);
+    const int st = 1 << ps.lt;
+#pragma unroll 1
+    for (int i = 0; i < S::E / 16; i++) {
+      const int g = (int)threadIdx.x + i * S::T;
+      const int a0 = ps.first(g);
+      u64 v[16];
 #pragma unroll
-    for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
+      for (int j = 0; j < 16; j++) v[j] = sm[pad(a0 + j * st)];
+      gs_group<4, 0, false, false>(v, t.inv, ps.base(g), t);
+#pragma unroll
+      for (int j = 0; j < 16; j++) sm[pad(a0 + j * st)] = v[j];
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  static_for<0, S::NHEAD>([&](auto pc) {
-    constexpr int P = S::NHEAD - 1 - decltype(pc)::value;  // NHEAD-1 .. 0
-    inv_pass<S, P, FOLD>(sm, t, tw_mult, out);
-    if constexpr (P > 0) __syncthreads();
-  });
+}
+
+// Last inverse pass (stages FIRSTK-1 .. 0) from shared memory to `out`,
+// coalesced.  fold: whole transform, n^-1 folded into stage 0, canonical
+// output; otherwise lazy [0, 2q).
+template <class S>
+__device__ __forceinline__ void inv_last(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, bool fold) {
+  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+#pragma unroll 1
+  for (int i = 0; i < G; i++) {
+    const int g = (int)threadIdx.x + i * S::T;
+    u64 v[1 << KK];
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];
+    if (fold)
+      gs_group<KK, 0, false, true>(v, t.inv, tw_mult, t);
+    else
+      gs_group<KK, 0, false, false>(v, t.inv, tw_mult, t);
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) out[g + j * TMIN] = v[j];
+  }
 }
 
 // Register groups of 16 consecutive words <-> global memory (32-byte vectors).
@@ -364,8 +358,7 @@ __device__ __forceinline__ void store16(const u64 (&v)[16], u64* p) {
 
 // Resident CTAs per SM the register budget is sized for: 512 threads per SM
 // (128 registers per thread) for the 32-words-per-thread shapes, 384 threads
-// (about 170 registers) for the 16-words-per-thread shapes, whose fused
-// pointwise step holds two 16-word groups.
+// (about 170 registers) for the 16-words-per-thread shapes.
 template <int LOGN, int E>
 constexpr int min_blocks() {
   constexpr int budget = E >= 32 ? 512 : 384;
@@ -381,7 +374,8 @@ __device__ __forceinline__ J fetch_job(const J* jobs, const J& one, int jid) {
 // Kernels.  Jobs come from a device array (persistent loop over
 // blockIdx.x, blockIdx.x + gridDim.x, ...) or, for a single job, by value.
 // sub_log > 0: each job is split into 2^sub_log sub-blocks of 2^LOGN words
-// (transforms of 2^(LOGN + sub_log) words after / before the global passes).
+// (transforms of 2^(LOGN + sub_log) words after / before the global passes),
+// sub-block `sub` using twiddle multiplier 2^sub_log + sub.
 
 template <int LOGN, int E>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
@@ -389,28 +383,20 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
   using S = Shape<LOGN, E>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
+#pragma unroll 1
   for (int w = blockIdx.x; w < total; w += gridDim.x) {
     const vkcu_ntt_job job = fetch_job(jobs, one, w >> sub_log);
     const int sub = w & ((1 << sub_log) - 1);
     const Tw t = load_tw(job.tw);
     u64* out = reinterpret_cast<u64*>(job.out) + ((size_t)sub << LOGN);
-    if (sub_log == 0) {
-      fwd_head<S, true>(sm, reinterpret_cast<const u64*>(job.in), t, 1u);
-      fwd_last<S>(sm, t, 1u, [&](int g, u64(&v)[16]) {
+    const u64* in = sub_log ? out : reinterpret_cast<const u64*>(job.in);
+    const u32 tw_mult = (1u << sub_log) + sub;
+    fwd_first<S>(sm, in, t, tw_mult);
+    fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
 #pragma unroll
-        for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
-        store16(v, out + 16 * g);
-      });
-    } else {
-      const u32 tw_mult = (1u << sub_log) + sub;
-      fwd_head<S, false>(sm, out, t, tw_mult);
-      fwd_last<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
-#pragma unroll
-        for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
-        store16(v, out + 16 * g);
-      });
-    }
-    __syncthreads();
+      for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+      store16(v, out + 16 * g);
+    });
   }
 }
 
@@ -420,6 +406,7 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
   using S = Shape<LOGN, E>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
+#pragma unroll 1
   for (int w = blockIdx.x; w < total; w += gridDim.x) {
     const vkcu_ntt_job job = fetch_job(jobs, one, w >> sub_log);
     const int sub = w & ((1 << sub_log) - 1);
@@ -427,60 +414,63 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     const u64* in = reinterpret_cast<const u64*>(job.in) + ((size_t)sub << LOGN);
     u64* out = reinterpret_cast<u64*>(job.out) + ((size_t)sub << LOGN);
     const u32 tw_mult = (1u << sub_log) + sub;
-    auto first = [&](int g, u64(&v)[16]) {
+    // first inverse pass (global stage m = n/2 first, exact rule) from global
+#pragma unroll 1
+    for (int i = 0; i < S::E / 16; i++) {
+      const int g = (int)threadIdx.x + i * S::T;
+      u64 v[16];
       load16(v, in + 16 * g);
       gs_group<4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
-    };
-    if (sub_log == 0)
-      inv_ntt<S, true>(sm, t, 1u, out, first);
-    else
-      inv_ntt<S, false>(sm, t, tw_mult, out, first);
+#pragma unroll
+      for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
+    }
+    __syncthreads();
+    inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
+    inv_last<S>(sm, t, tw_mult, out, sub_log == 0);
     __syncthreads();
   }
 }
 
-// Fused c = INTT(NTT(a) . NTT(b)).  NTT(b) goes to job.scratch (canonical);
-// NTT(a)'s last pass, the pointwise product (NTT(b) read back at the words
-// this thread wrote) and the first inverse pass share registers, group by
-// group; the inverse writes c.  a is prefetched into L2 while NTT(b) runs.
+// Fused c = INTT(NTT(a) . NTT(b)).  Phase 0 transforms b and parks NTT(b)
+// (canonical) in job.scratch; phase 1 transforms a with the same code, and its
+// last pass multiplies by NTT(b) (read back at the words this thread wrote)
+// into shared memory; the inverse transform then writes c.  a is prefetched
+// into L2 while b is transformed, the next job's b while a is.
 template <int LOGN, int E>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one) {
   using S = Shape<LOGN, E>;
   extern __shared__ u64 sm[];
+  constexpr unsigned kChunk = (unsigned)(S::N * 8 / 4);
+#pragma unroll 1
   for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
     const vkcu_poly_job job = fetch_job(jobs, one, w);
     const Tw t = load_tw(job.tw);
     u64* scratch = reinterpret_cast<u64*>(job.scratch);
-    if (threadIdx.x < 4) {
-      constexpr unsigned chunk = (unsigned)(S::N * 8 / 4);
-      prefetch_l2(reinterpret_cast<const char*>(job.a) + threadIdx.x * chunk, chunk);
+    if (threadIdx.x < 4) prefetch_l2(reinterpret_cast<const char*>(job.a) + threadIdx.x * kChunk, kChunk);
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ph++) {
+      fwd_first<S>(sm, reinterpret_cast<const u64*>(ph ? job.a : job.b), t, 1u);
+      if (ph == 1 && w + (int)gridDim.x < njobs && threadIdx.x < 4) {
+        const vkcu_poly_job nx = fetch_job(jobs, one, w + (int)gridDim.x);
+        prefetch_l2(reinterpret_cast<const char*>(nx.b) + threadIdx.x * kChunk, kChunk);
+      }
+      fwd_passes<S>(sm, t, 1u, [&](int g, u64(&v)[16]) {
+        if (ph == 0) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+          store16(v, scratch + 16 * g);
+        } else {
+          u64 bh[16];
+          load16(bh, scratch + 16 * g);
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            sm[pad(16 * g + j)] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+        }
+      });
     }
-    fwd_head<S, true>(sm, reinterpret_cast<const u64*>(job.b), t, 1u);
-    fwd_last<S>(sm, t, 1u, [&](int g, u64(&v)[16]) {
-#pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
-      store16(v, scratch + 16 * g);
-    });
-    __syncthreads();
-    fwd_head<S, true>(sm, reinterpret_cast<const u64*>(job.a), t, 1u);
-    if (w + (int)gridDim.x < njobs && threadIdx.x < 4) {
-      const vkcu_poly_job nx = fetch_job(jobs, one, w + (int)gridDim.x);
-      constexpr unsigned chunk = (unsigned)(S::N * 8 / 4);
-      prefetch_l2(reinterpret_cast<const char*>(nx.b) + threadIdx.x * chunk, chunk);
-    }
-    // The first inverse pass reads its words from registers and writes them
-    // to the same shared-memory slots the last forward pass read them from.
-    inv_ntt<S, true>(sm, t, 1u, reinterpret_cast<u64*>(job.c), [&](int g, u64(&v)[16]) {
-#pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = sm[pad(16 * g + j)];
-      ct_group<4, 0, 0>(v, t.fwd, (u32)(S::N / 16) + (u32)g, t);
-      u64 bh[16];
-      load16(bh, scratch + 16 * g);
-#pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
-      gs_group<4, 0, false, false>(v, t.inv, (u32)(S::N / 16) + (u32)g, t);
-    });
+    inv_passes<S>(sm, t, 1u, S::HEAD);
+    inv_last<S>(sm, t, 1u, reinterpret_cast<u64*>(job.c), true);
     __syncthreads();
   }
 }
