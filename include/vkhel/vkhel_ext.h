@@ -92,6 +92,21 @@ int vkhel_vector_polymul(const struct vkhel_vector *a,
 		const struct vkhel_vector *b, struct vkhel_vector *result,
 		struct vkhel_ntt_tables *ntt);
 
+/* Same product as vkhel_vector_polymul without allocating any device memory
+ * (no counterpart in the reference).  For callers that may not allocate at
+ * the call site -- e.g. while a stream is being captured into a CUDA graph, or
+ * inside another component's fixed memory budget -- the kernel's NTT(b)
+ * scratch is a static device array of 16384 words (128 KiB per device, kept
+ * until exit) instead of a pool buffer.  Needs 256 <= n <= 16384 and the
+ * tables already resident on the context (any earlier transform, polymul or
+ * batch call with them); rejects other sizes with VKHEL_ERR_UNSUPPORTED.
+ * All calls share the array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture.  Synchronous; returns a status. */
+int vkhel_vector_polymul_noalloc(const struct vkhel_vector *a,
+		const struct vkhel_vector *b, struct vkhel_vector *result,
+		const struct vkhel_ntt_tables *ntt);
+
 /* ---- batched polynomial multiply ----
  * A batch is a fixed list of limb products, built once, committed (the job
  * table is uploaded and, with VKHEL_BATCH_GRAPH, the launch sequence is

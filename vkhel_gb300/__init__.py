@@ -71,6 +71,7 @@ _SIGNATURES = [
     ("vkhel_ntt_tables_dbgprint", None, [vp]),
     ("vkhel_vector_elemfma_canonical", None, [vp, vp, vp, u64, u64]),
     ("vkhel_vector_polymul", ctypes.c_int, [vp, vp, vp, vp]),
+    ("vkhel_vector_polymul_noalloc", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_batch_create", vp, [vp]),
     ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
@@ -338,6 +339,11 @@ def inverse_transform(a, res, tables): _op("vkhel_vector_inverse_transform", a, 
 
 def polymul(a, b, res, tables):
     _status(res.ctx.ptr, lib().vkhel_vector_polymul(a.ptr, b.ptr, res.ptr, tables.ptr))
+
+
+def polymul_noalloc(a, b, res, tables):
+    """vkhel_vector_polymul_noalloc: same product, scratch in a static device array."""
+    _status(res.ctx.ptr, lib().vkhel_vector_polymul_noalloc(a.ptr, b.ptr, res.ptr, tables.ptr))
 
 
 def launch_count():

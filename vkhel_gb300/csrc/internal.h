@@ -11,6 +11,15 @@
 #include "../../include/vkhel/vkhel_ext.h"
 #include "kernels.h"
 
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* CUDA translation units compile with hidden visibility; public entry points
+ * defined there are marked with this (the version script then keeps only
+ * vkhel_* symbols). */
+#define VKHEL_EXPORT __attribute__((visibility("default")))
+
 /* Device copy of one (n, q, w) table set, cached in a context. */
 struct vkh_devtab {
 	struct vkh_devtab *next;
@@ -72,5 +81,11 @@ void vkh_dev_free(struct vkhel_ctx *ctx, void *ptr, uint64_t bytes);
 int vkh_devtab_get(struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t,
 		const struct vkh_devtab **out);
 void vkh_devtab_release_all(struct vkhel_ctx *ctx);
+/* Lookup only: NULL when (n, q, w) has no device copy in ctx yet. */
+const struct vkh_devtab *vkh_devtab_find(const struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t);
+
+#ifdef __cplusplus
+}
+#endif
 
 #endif

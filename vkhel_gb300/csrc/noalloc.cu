@@ -1,0 +1,91 @@
+// Fused polynomial multiply for callers that cannot allocate device memory.
+//
+// vkhel_vector_polymul parks NTT(b) in the result vector, or in a temporary
+// buffer from the context's pool when the result aliases a.  Some callers may
+// not allocate at all at the point where they multiply: code that runs while
+// a stream is being captured into a CUDA graph (allocation calls are not
+// allowed there), code inside another library's memory budget that owns all
+// of the device memory it may touch, or latency-critical serving paths that
+// must not call into the allocator.  vkhel_vector_polymul_noalloc runs the
+// same kernel (k_polymul) with its scratch in this file's static device array
+// instead, so it allocates nothing: the caller passes inputs and outputs.
+//
+// Limits and rules:
+//   * degree 256 <= n <= kNoallocMaxWords (16384): the fused range; the
+//     scratch array is kNoallocMaxWords words (128 KiB) on every device that
+//     loads libvkhel, held until the process exits;
+//   * the twiddle tables must already be resident on the context (any
+//     transform, polymul or batch call with them uploads them); otherwise the
+//     call fails instead of uploading (which would allocate);
+//   * every call on a device shares the one array and the kernel overwrites
+//     the n words it uses before reading them (nothing needs clearing), so
+//     calls that overlap on the GPU -- two contexts or threads running it at
+//     once -- race on the array; calls must not overlap;
+//   * the first call on each device resolves the array's device address with
+//     cudaGetSymbolAddress (host code cannot use the array's name as a device
+//     pointer); make that first call before any stream capture.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "internal.h"
+
+namespace {
+
+constexpr unsigned long long kNoallocMaxWords = 16384;
+
+__device__ __align__(256) unsigned long long g_polymul_scratch[kNoallocMaxWords];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+void* g_scratch_addr[kMaxDevices];
+
+// Device address of g_polymul_scratch on `device`, resolved once per device
+// with that device current.
+int scratch_address(int device, void** out) {
+  if (device < 0 || device >= kMaxDevices) return (int)cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  if (!g_scratch_addr[device]) {
+    int prev = -1;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e == cudaSuccess && prev != device) e = cudaSetDevice(device);
+    void* p = nullptr;
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_polymul_scratch);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return (int)e;
+    g_scratch_addr[device] = p;
+  }
+  *out = g_scratch_addr[device];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" VKHEL_EXPORT int vkhel_vector_polymul_noalloc(const struct vkhel_vector* a, const struct vkhel_vector* b,
+                                            struct vkhel_vector* result, const struct vkhel_ntt_tables* t) {
+  if (!a || !b || !result || !t)
+    return vkh_fail(result ? result->ctx : NULL, VKHEL_ERR_INVALID_ARGUMENT, "polymul_noalloc: NULL argument");
+  struct vkhel_ctx* ctx = result->ctx;
+  if (a->ctx != ctx || b->ctx != ctx)
+    return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "polymul_noalloc: vectors belong to different contexts");
+  if (t->n > kNoallocMaxWords || t->log_n < 8 || t->log_n > vkcu_max_fused_log_n())
+    return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED,
+                    "polymul_noalloc: n=%llu outside 256..%llu (static scratch of %llu words)",
+                    (unsigned long long)t->n, kNoallocMaxWords, kNoallocMaxWords);
+  if (t->q < 3 || t->q >= (1ull << 62))
+    return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "polymul_noalloc: q outside [3, 2^62)");
+  if (a->length < t->n || b->length < t->n || result->length < t->n)
+    return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "polymul_noalloc: vectors shorter than n");
+  const struct vkh_devtab* d = vkh_devtab_find(ctx, t);
+  if (!d)
+    return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT,
+                    "polymul_noalloc: tables not resident on this context (run any transform or polymul "
+                    "with them first)");
+  void* scratch = nullptr;
+  int e = scratch_address(ctx->device, &scratch);
+  if (e) return vkh_cuda(ctx, e, "polymul_noalloc: scratch address");
+  const vkcu_poly_job job = {a->dev, b->dev, result->dev, static_cast<uint64_t*>(scratch), d->dev_set};
+  e = vkcu_polymul(ctx->stream, nullptr, 1, &job, t->log_n, ctx->sms);
+  if (!e) e = vkcu_sync(ctx->stream);
+  return vkh_cuda(ctx, e, "polymul_noalloc");
+}

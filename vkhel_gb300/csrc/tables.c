@@ -195,6 +195,13 @@ int vkh_devtab_get(struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t,
 	return VKHEL_OK;
 }
 
+const struct vkh_devtab *vkh_devtab_find(const struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t) {
+	for (const struct vkh_devtab *d = ctx->tabs; d; d = d->next)
+		if (d->n == t->n && d->q == t->q && d->w == t->w)
+			return d;
+	return NULL;
+}
+
 void vkh_devtab_release_all(struct vkhel_ctx *ctx) {
 	struct vkh_devtab *d = ctx->tabs;
 	while (d) {
