@@ -161,6 +161,95 @@ def cpu_baseline_sample(qs, ws, a, b, budget_s=10.0):
                       f"{dt:.1f} s, oracle/oracle.c -O3, OpenMP over limbs"}
 
 
+def serving_sweep(vk, torch, rates=(1000, 4000, 16000, None), seconds=1.0, payloads=32, seed=4):
+    """Poisson arrivals of polymul requests (n = 2^k, k uniform in 12..17,
+    limbs uniform in 1..24, operands uniform mod each prime, seed 4) into a
+    vkhel server with a 40 GB budget; `None` = all requests at once
+    (saturation).  Returns the per-rate results and the plain per-call path."""
+    from vkhel_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    tabs = {}
+    for k in range(12, 18):
+        n = 1 << k
+        qs = workloads.ntt_primes(n, 24)
+        tabs[n] = [(q, vk.NttTables(n, q, workloads.root_for(n, q))) for q in qs]
+    pay = []
+    for _ in range(payloads):
+        n = 1 << int(rng.integers(12, 18))
+        limbs = int(rng.integers(1, 25))
+        tq = tabs[n][:limbs]
+        a = torch.empty(limbs * n, dtype=torch.int64).pin_memory()
+        b = torch.empty(limbs * n, dtype=torch.int64).pin_memory()
+        c = torch.empty(limbs * n, dtype=torch.int64).pin_memory()
+        a.numpy().view(np.uint64)[:] = np.concatenate([workloads.uniform(rng, q, n) for q, _ in tq])
+        b.numpy().view(np.uint64)[:] = np.concatenate([workloads.uniform(rng, q, n) for q, _ in tq])
+        pay.append((n, limbs, [t for _, t in tq], a, b, c))
+    mean_limbs = statistics.mean(p[1] for p in pay)
+    out = {"workload": f"{payloads} distinct requests reused round-robin: n = 2^k, k uniform in 12..17, "
+                       f"limbs uniform in 1..24 (mean {mean_limbs:.1f}), 60-bit primes, seed {seed}; "
+                       "pinned host operands; 40 GB device budget",
+           "rates": []}
+    with vk.Server(device_budget=40 << 30, max_batch_limbs=512, max_inflight_batches=3) as srv:
+        for p_ in pay:  # warm-up: table uploads, pool growth
+            srv.wait(srv.submit(p_[2], p_[3], p_[4], p_[5]))
+        for rate in rates:
+            count = int(min(6000, (rate or 20000) * seconds)) if rate else 2000
+            gaps = rng.exponential(1.0 / rate, size=count) if rate else np.zeros(count)
+            srv.reset_stats()
+            ids = []
+            t0 = time.perf_counter()
+            due = t0
+            limbs = 0
+            for i in range(count):
+                due += gaps[i]
+                while True:
+                    lag = due - time.perf_counter()
+                    if lag <= 0:
+                        break
+                    if lag > 2e-4:
+                        time.sleep(lag - 1e-4)
+                p_ = pay[i % payloads]
+                ids.append(srv.submit(p_[2], p_[3], p_[4], p_[5]))
+                limbs += p_[1]
+            fails = sum(srv.wait(r) != 0 for r in ids)
+            st = srv.stats()
+            out["rates"].append({
+                "offered_req_per_s": rate if rate else "saturation", "requests": count,
+                "achieved_req_per_s": st["completed"] / st["span_s"] if st["span_s"] else None,
+                "limb_polymul_per_s": limbs / st["span_s"] if st["span_s"] else None,
+                "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                "micro_batches": st["batches"], "failed": fails})
+    # plain per-call path: upload, forward x2, elemmul, inverse, download per limb
+    ctx = vk.Context()
+    lat = []
+    for n, limbs, tl, a, b, c in pay[:8]:
+        va, vb, vc = vk.Vector(ctx, n), vk.Vector(ctx, n), vk.Vector(ctx, n)
+        an, bn = a.numpy().view(np.uint64), b.numpy().view(np.uint64)
+        t0 = time.perf_counter()
+        for k in range(limbs):
+            va.upload(an[k * n:(k + 1) * n])
+            vb.upload(bn[k * n:(k + 1) * n])
+            vk.forward_transform(va, va, tl[k])
+            vk.forward_transform(vb, vb, tl[k])
+            vk.elemmul(va, vb, vc, tl[k].q)
+            vk.inverse_transform(vc, vc, tl[k])
+            vc.download()
+        lat.append(time.perf_counter() - t0)
+    ctx.close()
+    out["plain"] = {"req_per_s": len(lat) / sum(lat), "latency_ms_p50": 1e3 * statistics.median(lat),
+                    "requests": len(lat), "path": "per limb: upload a, b; forward x2; elemmul; inverse; download"}
+    sat = out["rates"][-1]["achieved_req_per_s"]
+    out["served_vs_plain"] = sat / out["plain"]["req_per_s"] if sat else None
+    # spot-check results against the oracle
+    from oracle import pyoracle
+    orc = pyoracle.load()
+    for n, limbs, tl, a, b, c in pay[:3]:
+        an, bn, cn = a.numpy().view(np.uint64), b.numpy().view(np.uint64), c.numpy().view(np.uint64)
+        ref, _ = orc.polymul(an[:n], bn[:n], n, tl[0].q, tl[0].w)
+        assert np.array_equal(cn[:n], ref), "serving result differs from the oracle"
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -168,6 +257,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
     ap.add_argument("--profile", action="store_true",
                     help="small profiling case: build the batch, launch it --steps times, print nothing else")
     args = ap.parse_args()
@@ -381,6 +471,8 @@ def main():
         "batch_latency_ms_p50": statistics.median(iso_ms),
         "batch_latency_ms_p99": pct(iso_ms, 0.99),
     }
+    if rank == 0 and not args.no_serve:
+        result["serving"] = serving_sweep(vk, torch)
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline_sample(qs, ws, a_h, b_h)
     if rank == 0:

@@ -139,6 +139,41 @@ uint32_t vkhel_batch_jobs(const struct vkhel_batch *batch);
 uint32_t vkhel_batch_kernels(const struct vkhel_batch *batch);
 void vkhel_batch_destroy(struct vkhel_batch *batch);
 
+/* ---- serving: continuous batching of polynomial-multiply requests ----
+ * A server owns a private context (device VKHEL_DEVICE), three streams and a
+ * scheduler thread.  Requests (limbs limb products of one degree with host
+ * operands a, b and host result c, limb-major, limbs * n words each) can be
+ * submitted from any thread; they are admitted in arrival order while the
+ * device budget allows, grouped into micro-batches of mixed degrees, and run
+ * with uploads, compute and downloads of consecutive micro-batches
+ * overlapping.  Host buffers must stay valid until the request is waited for;
+ * pinned host memory makes the copies asynchronous.  Each result equals the
+ * plain API's (forward, forward, elemmul, inverse per limb). */
+struct vkhel_server;
+struct vkhel_server_config {
+	uint64_t device_budget;        /* bytes for in-flight requests (0: 40 GiB) */
+	uint32_t max_batch_limbs;      /* limb products per micro-batch (0: 1024) */
+	uint32_t max_inflight_batches; /* micro-batches on the device at once (0: 3) */
+};
+struct vkhel_server_stats {
+	uint64_t submitted, completed, failed, batches, limbs;
+	double span_s;                 /* first submission to last completion */
+	double mean_ms, p50_ms, p99_ms, max_ms; /* request latency, submit -> done */
+};
+struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg);
+/* Returns a request id > 0, or -status. */
+int64_t vkhel_server_submit(struct vkhel_server *s,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b, uint64_t *c);
+/* Waits up to timeout_ms for request `id`; returns its status, or
+ * VKHEL_ERR_TIMEOUT (the request stays pending and can be waited for again).
+ * After a non-timeout return the id is collected and cannot be waited again. */
+int vkhel_server_wait(struct vkhel_server *s, int64_t id, uint32_t timeout_ms);
+int vkhel_server_stats(struct vkhel_server *s, struct vkhel_server_stats *out);
+int vkhel_server_reset_stats(struct vkhel_server *s);
+/* Runs the remaining queue to completion, then frees everything. */
+void vkhel_server_destroy(struct vkhel_server *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,6 +81,12 @@ _SIGNATURES = [
     ("vkhel_batch_jobs", u32, [vp]),
     ("vkhel_batch_kernels", u32, [vp]),
     ("vkhel_batch_destroy", None, [vp]),
+    ("vkhel_server_create", vp, [vp]),
+    ("vkhel_server_submit", ctypes.c_int64, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_server_wait", ctypes.c_int, [vp, ctypes.c_int64, u32]),
+    ("vkhel_server_stats", ctypes.c_int, [vp, vp]),
+    ("vkhel_server_reset_stats", ctypes.c_int, [vp]),
+    ("vkhel_server_destroy", None, [vp]),
 ]
 
 STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "OUT_OF_MEMORY", 3: "BUDGET", 4: "DEVICE",
@@ -397,3 +403,85 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device_budget", ctypes.c_uint64), ("max_batch_limbs", ctypes.c_uint32),
+                ("max_inflight_batches", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("limbs", ctypes.c_uint64), ("span_s", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Server:
+    """vkhel_server: continuous batching of polynomial-multiply requests.
+
+    submit() takes NttTables per limb and host uint64 arrays (limb-major,
+    limbs * n words); the arrays are kept referenced until wait() returns.
+    """
+
+    def __init__(self, device_budget=0, max_batch_limbs=0, max_inflight_batches=0):
+        cfg = ServerConfig(int(device_budget), int(max_batch_limbs), int(max_inflight_batches))
+        lib().vkhel_ctx_clear_error(None)
+        self.ptr = lib().vkhel_server_create(ctypes.byref(cfg))
+        if not self.ptr:
+            code, msg = last_error(None)
+            raise VkhelError(code or 4, msg)
+        self._pending = {}
+
+    def submit(self, tables, a, b, c):
+        arr = (vp * len(tables))(*[t.ptr for t in tables])
+        rid = lib().vkhel_server_submit(self.ptr, arr, len(tables), _ptr(a), _ptr(b), _ptr(c))
+        if rid < 0:
+            code, msg = last_error(None)
+            lib().vkhel_ctx_clear_error(None)
+            raise VkhelError(-rid, msg)
+        self._pending[rid] = (tables, a, b, c)
+        return rid
+
+    def wait(self, rid, timeout_ms=60000):
+        st = lib().vkhel_server_wait(self.ptr, rid, int(timeout_ms))
+        if st != 6:  # not a timeout: the id is collected
+            self._pending.pop(rid, None)
+        return st
+
+    def stats(self):
+        s = ServerStats()
+        lib().vkhel_server_stats(self.ptr, ctypes.byref(s))
+        return s.as_dict()
+
+    def reset_stats(self):
+        lib().vkhel_server_reset_stats(self.ptr)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            lib().vkhel_server_destroy(self.ptr)
+            self.ptr = None
+            self._pending.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ptr(x):
+    """Host address of a numpy array or a torch tensor (pinned or not)."""
+    if isinstance(x, np.ndarray):
+        assert x.dtype == np.uint64 and x.flags.c_contiguous
+        return x.ctypes.data
+    return x.data_ptr()

@@ -25,7 +25,7 @@ ORACLE_LIB = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                      "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
-CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
+CC_FLAGS = ["-O2", "-std=gnu11", "-fPIC", "-pthread", "-Wall", "-Wextra", "-Wno-unused-parameter",
             "-I" + os.path.join(ROOT, "include")]
 
 

@@ -26,19 +26,13 @@ struct job_rec {
 	vkcu_poly_job job;
 };
 
-struct job_class {
-	uint32_t log_n;
-	uint32_t first, count;
-	int fused;
-};
-
 struct vkhel_batch {
 	struct vkhel_ctx *ctx;
 	struct job_rec *recs;
 	uint32_t njobs, cap;
 	int committed;
 	uint32_t flags;
-	struct job_class classes[MAX_CLASSES];
+	struct vkh_job_class classes[MAX_CLASSES];
 	uint32_t nclasses;
 	void *dev;             /* poly jobs, then 3 ntt-job arrays per composed class */
 	uint64_t dev_bytes;
@@ -139,29 +133,52 @@ static int cmp_rec(const void *x, const void *y) {
 	return (a->log_n > b->log_n) - (a->log_n < b->log_n);
 }
 
-/* Issue every class of the batch on the context stream. */
-static int issue(struct vkhel_batch *b) {
-	struct vkhel_ctx *ctx = b->ctx;
-	for (uint32_t k = 0; k < b->nclasses; k++) {
-		const struct job_class *cl = &b->classes[k];
+/* Launch the kernels of `nclasses` degree classes on `stream`: one fused
+ * polymul launch per class with 2^8 <= n <= 2^14, otherwise forward(b ->
+ * scratch), forward(a -> c), pointwise, inverse(c) over the class's slice of
+ * the ntt-job array (laid out at 3 * first: b jobs, a jobs, c jobs). */
+int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt,
+		const struct vkh_job_class *classes, uint32_t nclasses) {
+	for (uint32_t k = 0; k < nclasses; k++) {
+		const struct vkh_job_class *cl = &classes[k];
 		int e;
 		if (cl->fused) {
-			e = vkcu_polymul(ctx->stream, b->dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, ctx->sms);
+			e = vkcu_polymul(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, sms);
 		} else {
-			vkcu_ntt_job *nj = b->dev_ntt + 3 * (size_t) cl->first;
-			e = vkcu_ntt_forward(ctx->stream, nj, (int) cl->count, NULL, cl->log_n, ctx->sms);
+			const vkcu_ntt_job *nj = dev_ntt + 3 * (size_t) cl->first;
+			e = vkcu_ntt_forward(stream, nj, (int) cl->count, NULL, cl->log_n, sms);
 			if (!e)
-				e = vkcu_ntt_forward(ctx->stream, nj + cl->count, (int) cl->count, NULL, cl->log_n, ctx->sms);
+				e = vkcu_ntt_forward(stream, nj + cl->count, (int) cl->count, NULL, cl->log_n, sms);
 			if (!e)
-				e = vkcu_pointwise(ctx->stream, b->dev_poly + cl->first, (int) cl->count, cl->log_n, ctx->sms);
+				e = vkcu_pointwise(stream, dev_poly + cl->first, (int) cl->count, cl->log_n, sms);
 			if (!e)
-				e = vkcu_ntt_inverse(ctx->stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n,
-						ctx->sms);
+				e = vkcu_ntt_inverse(stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n, sms);
 		}
 		if (e)
 			return e;
 	}
 	return 0;
+}
+
+/* Fill the three ntt-job arrays of every composed class from the poly jobs. */
+void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struct vkh_job_class *classes,
+		uint32_t nclasses) {
+	for (uint32_t k = 0; k < nclasses; k++) {
+		const struct vkh_job_class *cl = &classes[k];
+		if (cl->fused)
+			continue;
+		vkcu_ntt_job *nj = ntt + 3 * (size_t) cl->first;
+		for (uint32_t i = 0; i < cl->count; i++) {
+			const vkcu_poly_job *j = &poly[cl->first + i];
+			nj[i] = (vkcu_ntt_job){j->b, j->scratch, j->tw};
+			nj[cl->count + i] = (vkcu_ntt_job){j->a, j->c, j->tw};
+			nj[2 * cl->count + i] = (vkcu_ntt_job){j->c, j->c, j->tw};
+		}
+	}
+}
+
+static int issue(struct vkhel_batch *b) {
+	return vkh_issue_classes(b->ctx->stream, b->ctx->sms, b->dev_poly, b->dev_ntt, b->classes, b->nclasses);
 }
 
 int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
@@ -182,7 +199,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 		if (b->nclasses == 0 || b->classes[b->nclasses - 1].log_n != r->log_n) {
 			if (b->nclasses == MAX_CLASSES)
 				return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_commit: too many degree classes");
-			struct job_class *cl = &b->classes[b->nclasses++];
+			struct vkh_job_class *cl = &b->classes[b->nclasses++];
 			cl->log_n = r->log_n;
 			cl->first = i;
 			cl->count = 0;
@@ -219,16 +236,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	vkcu_ntt_job *hn = (vkcu_ntt_job *) ((char *) host + ntt_off);
 	for (uint32_t i = 0; i < b->njobs; i++)
 		hp[i] = b->recs[i].job;
-	for (uint32_t k = 0; k < b->nclasses; k++) {
-		const struct job_class *cl = &b->classes[k];
-		vkcu_ntt_job *nj = hn + 3 * (size_t) cl->first;
-		for (uint32_t i = 0; i < cl->count; i++) {
-			const vkcu_poly_job *j = &hp[cl->first + i];
-			nj[i] = (vkcu_ntt_job){j->b, j->scratch, j->tw};
-			nj[cl->count + i] = (vkcu_ntt_job){j->a, j->c, j->tw};
-			nj[2 * cl->count + i] = (vkcu_ntt_job){j->c, j->c, j->tw};
-		}
-	}
+	vkh_fill_ntt_jobs(hp, hn, b->classes, b->nclasses);
 	int st = vkh_dev_alloc(ctx, b->dev_bytes, &b->dev);
 	if (st) {
 		free(host);

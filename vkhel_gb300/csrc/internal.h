@@ -81,6 +81,16 @@ void vkh_dev_free(struct vkhel_ctx *ctx, void *ptr, uint64_t bytes);
 int vkh_devtab_get(struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t,
 		const struct vkh_devtab **out);
 void vkh_devtab_release_all(struct vkhel_ctx *ctx);
+/* batch.c -- degree classes of a sorted job list, shared with the server */
+struct vkh_job_class {
+	uint32_t log_n;
+	uint32_t first, count;
+	int fused;
+};
+int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt,
+		const struct vkh_job_class *classes, uint32_t nclasses);
+void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struct vkh_job_class *classes,
+		uint32_t nclasses);
 /* Lookup only: NULL when (n, q, w) has no device copy in ctx yet. */
 const struct vkh_devtab *vkh_devtab_find(const struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t);
 

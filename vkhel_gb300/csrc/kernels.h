@@ -68,6 +68,12 @@ int vkcu_capture_begin(void *stream);
 int vkcu_capture_end(void *stream, void **exec);
 int vkcu_graph_launch(void *exec, void *stream);
 int vkcu_graph_destroy(void *exec);
+int vkcu_event_create(void **ev);
+int vkcu_event_destroy(void *ev);
+int vkcu_event_record(void *ev, void *stream);
+int vkcu_stream_wait(void *stream, void *ev);
+int vkcu_event_query(void *ev);
+int vkcu_host_is_pinned(const void *p);
 
 /* ---- element-wise kernels (elem.cu); `len` elements of `res` ---- */
 int vkcu_elemmul(void *stream, uint64_t *res, const uint64_t *a,

@@ -121,3 +121,38 @@ extern "C" int vkcu_graph_launch(void* exec, void* stream) {
 extern "C" int vkcu_graph_destroy(void* exec) {
   return exec ? (int)cudaGraphExecDestroy((cudaGraphExec_t)exec) : 0;
 }
+
+// ---- events: cross-stream ordering and completion polling (serving loop) ----
+extern "C" int vkcu_event_create(void** ev) {
+  cudaEvent_t e = nullptr;
+  const cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  *ev = e;
+  return (int)r;
+}
+
+extern "C" int vkcu_event_destroy(void* ev) { return ev ? (int)cudaEventDestroy((cudaEvent_t)ev) : 0; }
+
+extern "C" int vkcu_event_record(void* ev, void* stream) {
+  return (int)cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream);
+}
+
+extern "C" int vkcu_stream_wait(void* stream, void* ev) {
+  return (int)cudaStreamWaitEvent((cudaStream_t)stream, (cudaEvent_t)ev, 0);
+}
+
+// 0 = completed, 1 = not yet, anything else = CUDA error
+extern "C" int vkcu_event_query(void* ev) {
+  const cudaError_t r = cudaEventQuery((cudaEvent_t)ev);
+  if (r == cudaSuccess) return 0;
+  if (r == cudaErrorNotReady) return 1;
+  return (int)r;
+}
+
+extern "C" int vkcu_host_is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return a.type == cudaMemoryTypeHost;
+}

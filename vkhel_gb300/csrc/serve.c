@@ -1,0 +1,544 @@
+/*
+ * Serving loop: continuous batching of polynomial-multiply requests (no
+ * counterpart in the reference, whose calls block one at a time).
+ *
+ * Callers submit requests -- `limbs` limb products of degree n with host
+ * operands and a host result buffer -- from any thread and wait for them.  A
+ * scheduler thread owned by the server:
+ *   - admits requests in arrival order while the device-memory budget and a
+ *     free micro-batch slot allow (a request waits at the head of the queue
+ *     until enough in-flight memory is released);
+ *   - forms a micro-batch of up to max_batch_limbs limb products of any mix
+ *     of degrees, uploads its operands and job table on the input stream,
+ *     runs one kernel per degree class on the compute stream (the fused
+ *     polymul for 2^8 <= n <= 2^14, the composed transforms otherwise) and
+ *     downloads results on the output stream; the three streams are chained
+ *     by events, so while one micro-batch computes the next is uploaded and
+ *     the previous one downloaded;
+ *   - polls completion events, releases memory and wakes waiters; requests
+ *     that arrive while others run join the next micro-batch.
+ * Every limb product is computed exactly as in the plain API, so a request's
+ * result is the same alone and in any mix.  Latency = completion - submission
+ * (monotonic clock), recorded per request.  All device work happens on the
+ * server's own context and streams.
+ */
+#include <errno.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "internal.h"
+
+#define SRV_MAX_CLASSES 32
+
+struct srv_req {
+	struct srv_req *next;
+	int64_t id;
+	uint32_t limbs, log_n;
+	uint64_t n;
+	const uint64_t *a, *b;
+	uint64_t *c;
+	struct vkhel_ntt_tables **tables;
+	int state; /* 0 queued, 1 running, 2 finished */
+	int status;
+	double t_submit, t_done;
+	void *dev;
+	uint64_t dev_bytes;
+};
+
+struct srv_slot {
+	int busy;
+	void *ev_in, *ev_comp, *ev_done;
+	vkcu_poly_job *host_poly; /* pinned */
+	vkcu_ntt_job *host_ntt;   /* pinned, 3 per job */
+	void *dev_jobs;           /* poly jobs then ntt jobs */
+	struct srv_req **reqs;
+	uint32_t nreqs;
+};
+
+struct vkhel_server {
+	struct vkhel_ctx *ctx; /* private context: tables cache, pool, SM count */
+	void *s_in, *s_comp, *s_out;
+	uint64_t budget, bytes;
+	uint32_t max_limbs, nslots;
+	struct srv_slot *slots;
+	pthread_t thread;
+	pthread_mutex_t mu;
+	pthread_cond_t cv_work, cv_done;
+	int stop;
+	struct srv_req *q_head, *q_tail;
+	struct srv_req **by_id; /* index id - 1 */
+	int64_t next_id, cap_id;
+	double *lat_ms;
+	uint64_t nlat, cap_lat;
+	uint64_t submitted, completed, failed, batches, limbs_done;
+	double t_first, t_last;
+};
+
+static double now_s(void) {
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return (double) ts.tv_sec + 1e-9 * (double) ts.tv_nsec;
+}
+
+static int fused_log_n(uint32_t log_n) {
+	return log_n >= 8 && log_n <= vkcu_max_fused_log_n();
+}
+
+static uint64_t req_bytes(const struct srv_req *r) {
+	const uint64_t words = (uint64_t) r->limbs * r->n;
+	return 8 * words * (fused_log_n(r->log_n) ? 3 : 4);
+}
+
+static int cmp_job_log_n(const void *x, const void *y) {
+	const uint64_t a = *(const uint64_t *) x, b = *(const uint64_t *) y;
+	return (a > b) - (a < b);
+}
+
+/* Enqueue one micro-batch on the server streams (called without the lock). */
+static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
+	struct vkhel_ctx *ctx = s->ctx;
+	uint32_t njobs = 0;
+	/* keys: log_n in the high bits, running index in the low bits -> stable sort */
+	uint64_t *keys = malloc(sizeof(uint64_t) * (s->max_limbs + 64) * 2);
+	vkcu_poly_job *tmp = malloc(sizeof(vkcu_poly_job) * (s->max_limbs + 64) * 2);
+	int err = 0;
+	for (uint32_t i = 0; i < sl->nreqs; i++) {
+		struct srv_req *r = sl->reqs[i];
+		const uint64_t words = (uint64_t) r->limbs * r->n;
+		const int fused = fused_log_n(r->log_n);
+		int e = vkcu_alloc(ctx->pool, s->s_in, r->dev_bytes, &r->dev);
+		if (!e)
+			e = vkcu_h2d(s->s_in, r->dev, r->a, 8 * words);
+		if (!e)
+			e = vkcu_h2d(s->s_in, (uint64_t *) r->dev + words, r->b, 8 * words);
+		for (uint32_t k = 0; !e && k < r->limbs; k++) {
+			const struct vkh_devtab *d = NULL;
+			e = vkh_devtab_get(ctx, r->tables[k], &d);
+			if (e)
+				break;
+			uint64_t *base = r->dev;
+			vkcu_poly_job j;
+			j.a = base + (uint64_t) k * r->n;
+			j.b = base + words + (uint64_t) k * r->n;
+			j.c = base + 2 * words + (uint64_t) k * r->n;
+			j.scratch = fused ? j.c : base + 3 * words + (uint64_t) k * r->n;
+			j.tw = d->dev_set;
+			keys[njobs] = ((uint64_t) r->log_n << 40) | njobs;
+			tmp[njobs++] = j;
+		}
+		if (e) {
+			err = e == 2 /* cudaErrorMemoryAllocation */ || e == VKHEL_ERR_BUDGET || e == VKHEL_ERR_OUT_OF_MEMORY
+					? VKHEL_ERR_OUT_OF_MEMORY
+					: VKHEL_ERR_DEVICE;
+			break;
+		}
+	}
+	if (err) /* nothing of this micro-batch runs; its requests fail */
+		for (uint32_t i = 0; i < sl->nreqs; i++)
+			sl->reqs[i]->status = err;
+	struct vkh_job_class classes[SRV_MAX_CLASSES];
+	uint32_t nclasses = 0;
+	if (!err) {
+		qsort(keys, njobs, sizeof(uint64_t), cmp_job_log_n);
+		for (uint32_t i = 0; i < njobs; i++) {
+			const uint32_t log_n = (uint32_t) (keys[i] >> 40);
+			sl->host_poly[i] = tmp[keys[i] & 0xffffffffffull];
+			if (nclasses == 0 || classes[nclasses - 1].log_n != log_n) {
+				struct vkh_job_class *cl = &classes[nclasses++];
+				cl->log_n = log_n;
+				cl->first = i;
+				cl->count = 0;
+				cl->fused = fused_log_n(log_n);
+			}
+			classes[nclasses - 1].count++;
+		}
+		vkh_fill_ntt_jobs(sl->host_poly, sl->host_ntt, classes, nclasses);
+		vkcu_poly_job *dpoly = sl->dev_jobs;
+		vkcu_ntt_job *dntt = (vkcu_ntt_job *) ((char *) sl->dev_jobs + sizeof(vkcu_poly_job) * (s->max_limbs + 64) * 2);
+		int e = vkcu_h2d(s->s_in, dpoly, sl->host_poly, sizeof(vkcu_poly_job) * njobs);
+		if (!e)
+			e = vkcu_h2d(s->s_in, dntt, sl->host_ntt, sizeof(vkcu_ntt_job) * 3 * njobs);
+		if (!e)
+			e = vkcu_event_record(sl->ev_in, s->s_in);
+		if (!e)
+			e = vkcu_stream_wait(s->s_comp, sl->ev_in);
+		if (!e)
+			e = vkh_issue_classes(s->s_comp, ctx->sms, dpoly, dntt, classes, nclasses);
+		if (!e)
+			e = vkcu_event_record(sl->ev_comp, s->s_comp);
+		if (!e)
+			e = vkcu_stream_wait(s->s_out, sl->ev_comp);
+		for (uint32_t i = 0; !e && i < sl->nreqs; i++) {
+			struct srv_req *r = sl->reqs[i];
+			const uint64_t words = (uint64_t) r->limbs * r->n;
+			e = vkcu_d2h(s->s_out, r->c, (uint64_t *) r->dev + 2 * words, 8 * words);
+		}
+		if (e) {
+			for (uint32_t i = 0; i < sl->nreqs; i++)
+				sl->reqs[i]->status = VKHEL_ERR_DEVICE;
+		}
+	}
+	for (uint32_t i = 0; i < sl->nreqs; i++) {
+		struct srv_req *r = sl->reqs[i];
+		if (r->dev)
+			vkcu_free(s->s_out, r->dev); /* stream-ordered: after the download */
+		r->dev = NULL;
+	}
+	vkcu_event_record(sl->ev_done, s->s_out);
+	free(keys);
+	free(tmp);
+}
+
+/* Mark a finished slot's requests done (lock held). */
+static void finish_slot(struct vkhel_server *s, struct srv_slot *sl, int status) {
+	const double t = now_s();
+	for (uint32_t i = 0; i < sl->nreqs; i++) {
+		struct srv_req *r = sl->reqs[i];
+		if (r->status == 0 && status)
+			r->status = status;
+		r->state = 2;
+		r->t_done = t;
+		s->bytes -= r->dev_bytes;
+		if (r->status == 0) {
+			s->completed++;
+			s->limbs_done += r->limbs;
+			if (s->nlat == s->cap_lat) {
+				s->cap_lat = s->cap_lat ? 2 * s->cap_lat : 4096;
+				s->lat_ms = realloc(s->lat_ms, sizeof(double) * s->cap_lat);
+			}
+			s->lat_ms[s->nlat++] = 1e3 * (t - r->t_submit);
+			s->t_last = t;
+		} else {
+			s->failed++;
+		}
+	}
+	sl->nreqs = 0;
+	sl->busy = 0;
+	s->batches++;
+	pthread_cond_broadcast(&s->cv_done);
+}
+
+static void *scheduler(void *arg) {
+	struct vkhel_server *s = arg;
+	vkcu_set_device(s->ctx->device);
+	for (;;) {
+		int progressed = 0;
+		/* completions */
+		for (uint32_t k = 0; k < s->nslots; k++) {
+			struct srv_slot *sl = &s->slots[k];
+			if (!sl->busy)
+				continue;
+			const int q = vkcu_event_query(sl->ev_done);
+			if (q == 1)
+				continue;
+			pthread_mutex_lock(&s->mu);
+			finish_slot(s, sl, q == 0 ? 0 : VKHEL_ERR_DEVICE);
+			pthread_mutex_unlock(&s->mu);
+			progressed = 1;
+		}
+		/* admission */
+		pthread_mutex_lock(&s->mu);
+		struct srv_slot *free_slot = NULL;
+		int inflight = 0;
+		for (uint32_t k = 0; k < s->nslots; k++) {
+			if (s->slots[k].busy)
+				inflight++;
+			else if (!free_slot)
+				free_slot = &s->slots[k];
+		}
+		if (s->stop && !s->q_head && inflight == 0) {
+			pthread_mutex_unlock(&s->mu);
+			break;
+		}
+		uint32_t limbs = 0;
+		if (free_slot) {
+			while (s->q_head) {
+				struct srv_req *r = s->q_head;
+				if (free_slot->nreqs > 0 && limbs + r->limbs > s->max_limbs)
+					break;
+				if (s->budget && s->bytes + r->dev_bytes > s->budget && (inflight > 0 || free_slot->nreqs > 0))
+					break; /* wait for memory held by running requests */
+				s->q_head = r->next;
+				if (!s->q_head)
+					s->q_tail = NULL;
+				r->state = 1;
+				s->bytes += r->dev_bytes;
+				limbs += r->limbs;
+				free_slot->reqs[free_slot->nreqs++] = r;
+			}
+		}
+		if (free_slot && free_slot->nreqs) {
+			free_slot->busy = 1;
+			pthread_mutex_unlock(&s->mu);
+			launch_slot(s, free_slot);
+			progressed = 1;
+			continue;
+		}
+		if (!progressed) {
+			if (inflight == 0) {
+				while (!s->q_head && !s->stop)
+					pthread_cond_wait(&s->cv_work, &s->mu);
+				pthread_mutex_unlock(&s->mu);
+			} else {
+				pthread_mutex_unlock(&s->mu);
+				const struct timespec ts = {0, 20000}; /* 20 us between completion polls */
+				nanosleep(&ts, NULL);
+			}
+		} else {
+			pthread_mutex_unlock(&s->mu);
+		}
+	}
+	return NULL;
+}
+
+struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg) {
+	struct vkhel_server *s = calloc(1, sizeof(*s));
+	if (!s) {
+		vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "server: host allocation failed");
+		return NULL;
+	}
+	s->ctx = vkhel_ctx_create();
+	if (!s->ctx) {
+		free(s);
+		return NULL;
+	}
+	s->budget = cfg && cfg->device_budget ? cfg->device_budget : ((uint64_t) 40 << 30);
+	s->max_limbs = cfg && cfg->max_batch_limbs ? cfg->max_batch_limbs : 1024;
+	s->nslots = cfg && cfg->max_inflight_batches ? cfg->max_inflight_batches : 3;
+	s->slots = calloc(s->nslots, sizeof(*s->slots));
+	int e = !s->slots;
+	if (!e)
+		e = vkcu_stream_create(&s->s_in);
+	if (!e)
+		e = vkcu_stream_create(&s->s_comp);
+	if (!e)
+		e = vkcu_stream_create(&s->s_out);
+	const uint64_t cap = (uint64_t) s->max_limbs + 64;
+	for (uint32_t k = 0; !e && k < s->nslots; k++) {
+		struct srv_slot *sl = &s->slots[k];
+		sl->reqs = calloc(2 * cap, sizeof(*sl->reqs));
+		e = !sl->reqs;
+		if (!e)
+			e = vkcu_event_create(&sl->ev_in);
+		if (!e)
+			e = vkcu_event_create(&sl->ev_comp);
+		if (!e)
+			e = vkcu_event_create(&sl->ev_done);
+		if (!e)
+			e = vkcu_host_alloc((void **) &sl->host_poly, sizeof(vkcu_poly_job) * 2 * cap);
+		if (!e)
+			e = vkcu_host_alloc((void **) &sl->host_ntt, sizeof(vkcu_ntt_job) * 6 * cap);
+		if (!e)
+			e = vkh_dev_alloc(s->ctx, (sizeof(vkcu_poly_job) + 3 * sizeof(vkcu_ntt_job)) * 2 * cap, &sl->dev_jobs);
+	}
+	if (!e)
+		e = vkcu_sync(s->ctx->stream);
+	if (e) {
+		vkh_fail(NULL, VKHEL_ERR_DEVICE, "server: set-up failed (%d)", e);
+		vkhel_server_destroy(s);
+		return NULL;
+	}
+	pthread_mutex_init(&s->mu, NULL);
+	pthread_cond_init(&s->cv_work, NULL);
+	pthread_cond_init(&s->cv_done, NULL);
+	s->next_id = 1;
+	if (pthread_create(&s->thread, NULL, scheduler, s) != 0) {
+		vkh_fail(NULL, VKHEL_ERR_DEVICE, "server: thread creation failed");
+		s->thread = 0;
+		vkhel_server_destroy(s);
+		return NULL;
+	}
+	return s;
+}
+
+int64_t vkhel_server_submit(struct vkhel_server *s, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b, uint64_t *c) {
+	if (!s || !tables || !limbs || !a || !b || !c || !tables[0])
+		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit: bad arguments");
+	if (limbs > s->max_limbs)
+		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT,
+				"server_submit: %u limbs exceed the micro-batch size %u", limbs, s->max_limbs);
+	const uint64_t n = tables[0]->n;
+	for (uint32_t k = 0; k < limbs; k++) {
+		const struct vkhel_ntt_tables *t = tables[k];
+		if (!t || t->n != n || n < 2)
+			return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit: limb %u tables invalid", k);
+		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_fused_log_n() + 4)
+			return -vkh_fail(NULL, VKHEL_ERR_UNSUPPORTED, "server_submit: limb %u (n, q) unsupported", k);
+	}
+	struct srv_req *r = calloc(1, sizeof(*r));
+	struct vkhel_ntt_tables **tcopy = malloc(sizeof(*tcopy) * limbs);
+	if (!r || !tcopy) {
+		free(r);
+		free(tcopy);
+		return -vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "server_submit: host allocation failed");
+	}
+	memcpy(tcopy, tables, sizeof(*tcopy) * limbs);
+	r->tables = tcopy;
+	r->limbs = limbs;
+	r->n = n;
+	r->log_n = tables[0]->log_n;
+	r->a = a;
+	r->b = b;
+	r->c = c;
+	r->dev_bytes = req_bytes(r);
+	pthread_mutex_lock(&s->mu);
+	if (s->stop) {
+		pthread_mutex_unlock(&s->mu);
+		free(tcopy);
+		free(r);
+		return -vkh_fail(NULL, VKHEL_ERR_CANCELLED, "server_submit: server is stopping");
+	}
+	if (s->next_id > s->cap_id) {
+		const int64_t cap = s->cap_id ? 2 * s->cap_id : 4096;
+		struct srv_req **m = realloc(s->by_id, sizeof(*m) * (size_t) cap);
+		if (!m) {
+			pthread_mutex_unlock(&s->mu);
+			free(tcopy);
+			free(r);
+			return -vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "server_submit: host allocation failed");
+		}
+		s->by_id = m;
+		s->cap_id = cap;
+	}
+	r->id = s->next_id++;
+	s->by_id[r->id - 1] = r;
+	r->t_submit = now_s();
+	if (s->submitted++ == 0)
+		s->t_first = r->t_submit;
+	if (s->q_tail)
+		s->q_tail->next = r;
+	else
+		s->q_head = r;
+	s->q_tail = r;
+	pthread_cond_signal(&s->cv_work);
+	pthread_mutex_unlock(&s->mu);
+	return r->id;
+}
+
+int vkhel_server_wait(struct vkhel_server *s, int64_t id, uint32_t timeout_ms) {
+	if (!s || id < 1)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_wait: bad arguments");
+	struct timespec dl;
+	clock_gettime(CLOCK_REALTIME, &dl);
+	dl.tv_sec += timeout_ms / 1000;
+	dl.tv_nsec += (long) (timeout_ms % 1000) * 1000000L;
+	if (dl.tv_nsec >= 1000000000L) {
+		dl.tv_sec++;
+		dl.tv_nsec -= 1000000000L;
+	}
+	pthread_mutex_lock(&s->mu);
+	if (id >= s->next_id || !s->by_id[id - 1]) {
+		pthread_mutex_unlock(&s->mu);
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_wait: unknown or already collected id %lld",
+				(long long) id);
+	}
+	struct srv_req *r = s->by_id[id - 1];
+	while (r->state != 2) {
+		if (pthread_cond_timedwait(&s->cv_done, &s->mu, &dl) == ETIMEDOUT && r->state != 2) {
+			pthread_mutex_unlock(&s->mu);
+			return VKHEL_ERR_TIMEOUT;
+		}
+	}
+	const int st = r->status;
+	s->by_id[id - 1] = NULL;
+	pthread_mutex_unlock(&s->mu);
+	free(r->tables);
+	free(r);
+	return st;
+}
+
+static int cmp_double(const void *x, const void *y) {
+	const double a = *(const double *) x, b = *(const double *) y;
+	return (a > b) - (a < b);
+}
+
+int vkhel_server_stats(struct vkhel_server *s, struct vkhel_server_stats *out) {
+	if (!s || !out)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_stats: NULL argument");
+	memset(out, 0, sizeof(*out));
+	pthread_mutex_lock(&s->mu);
+	out->submitted = s->submitted;
+	out->completed = s->completed;
+	out->failed = s->failed;
+	out->batches = s->batches;
+	out->limbs = s->limbs_done;
+	out->span_s = s->completed ? s->t_last - s->t_first : 0;
+	const uint64_t n = s->nlat;
+	double *v = n ? malloc(sizeof(double) * n) : NULL;
+	if (v)
+		memcpy(v, s->lat_ms, sizeof(double) * n);
+	pthread_mutex_unlock(&s->mu);
+	if (v) {
+		qsort(v, n, sizeof(double), cmp_double);
+		double sum = 0;
+		for (uint64_t i = 0; i < n; i++)
+			sum += v[i];
+		out->mean_ms = sum / (double) n;
+		out->p50_ms = v[n / 2];
+		out->p99_ms = v[(uint64_t) (0.99 * (double) (n - 1))];
+		out->max_ms = v[n - 1];
+		free(v);
+	}
+	return VKHEL_OK;
+}
+
+int vkhel_server_reset_stats(struct vkhel_server *s) {
+	if (!s)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_reset_stats: NULL server");
+	pthread_mutex_lock(&s->mu);
+	s->nlat = 0;
+	s->submitted = s->completed = s->failed = s->batches = s->limbs_done = 0;
+	s->t_first = s->t_last = 0;
+	pthread_mutex_unlock(&s->mu);
+	return VKHEL_OK;
+}
+
+/* Drains: queued requests still run; then every resource is released.
+ * Requests never waited for are freed here. */
+void vkhel_server_destroy(struct vkhel_server *s) {
+	if (!s)
+		return;
+	if (s->thread) {
+		pthread_mutex_lock(&s->mu);
+		s->stop = 1;
+		pthread_cond_broadcast(&s->cv_work);
+		pthread_mutex_unlock(&s->mu);
+		pthread_join(s->thread, NULL);
+		pthread_mutex_destroy(&s->mu);
+		pthread_cond_destroy(&s->cv_work);
+		pthread_cond_destroy(&s->cv_done);
+	}
+	void *streams[3] = {s->s_in, s->s_comp, s->s_out};
+	for (int i = 0; i < 3; i++)
+		if (streams[i])
+			vkcu_sync(streams[i]);
+	for (uint32_t k = 0; s->slots && k < s->nslots; k++) {
+		struct srv_slot *sl = &s->slots[k];
+		vkcu_event_destroy(sl->ev_in);
+		vkcu_event_destroy(sl->ev_comp);
+		vkcu_event_destroy(sl->ev_done);
+		vkcu_host_free(sl->host_poly);
+		vkcu_host_free(sl->host_ntt);
+		if (sl->dev_jobs)
+			vkh_dev_free(s->ctx, sl->dev_jobs, 0);
+		free(sl->reqs);
+	}
+	for (int i = 0; i < 3; i++)
+		if (streams[i])
+			vkcu_stream_destroy(streams[i]);
+	for (int64_t i = 0; i + 1 < s->next_id; i++) {
+		if (s->by_id[i]) {
+			free(s->by_id[i]->tables);
+			free(s->by_id[i]);
+		}
+	}
+	if (s->ctx)
+		vkhel_ctx_destroy(s->ctx);
+	free(s->slots);
+	free(s->by_id);
+	free(s->lat_ms);
+	free(s);
+}
