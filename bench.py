@@ -250,6 +250,87 @@ def serving_sweep(vk, torch, rates=(1000, 4000, 16000, None), seconds=1.0, paylo
     return out
 
 
+def batch_rate(vk, ctx, torch, jobs, reps=20):
+    """Commit `jobs` = [(tables, a_vec, b_vec, c_vec)] as one graph batch and
+    time `reps` launches with CUDA events; returns seconds per launch."""
+    bt = vk.Batch(ctx)
+    for tabs, va, vb, vc in jobs:
+        bt.add_polymul(tabs, va, vb, vc)
+    bt.commit(graph=True)
+    st = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(3):
+        bt.launch()
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        bt.launch()
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3 / reps, bt.kernels
+
+
+def extra_configs(vk, torch):
+    """The single-limb batch (n = 65536, 64 polynomials, seed 1) and the ragged
+    batch (512 instances, n = 2^k with k uniform in 12..16, limbs uniform in
+    1..16, seed 3): batched launch vs the plain per-call path."""
+    from oracle import pyoracle
+    from vkhel_gb300 import workloads
+    orc = pyoracle.load()
+    out = {}
+    ctx = vk.Context()
+    # single-limb batch
+    n, count = 65536, 64
+    qs, ws, a, b = workloads.rns_batch(n, 1, count, seed=1)
+    t = vk.NttTables(n, qs[0], ws[0])
+    jobs = [([t], vk.Vector(ctx, a[i, 0]), vk.Vector(ctx, b[i, 0]), vk.Vector(ctx, n)) for i in range(count)]
+    sec, kernels = batch_rate(vk, ctx, torch, jobs)
+    ref, _ = orc.polymul(a[0, 0], b[0, 0], n, qs[0], ws[0])
+    assert np.array_equal(jobs[0][3].download(), ref), "single-limb batch differs from the oracle"
+    t0 = time.perf_counter()
+    for i in range(4):
+        _, va, vb, vc = jobs[i]
+        vk.forward_transform(va, va, t)
+        vk.forward_transform(vb, vb, t)
+        vk.elemmul(va, vb, vc, qs[0])
+        vk.inverse_transform(vc, vc, t)
+    plain = 4 / (time.perf_counter() - t0)
+    out["single_limb_batch"] = {"workload": f"n={n}, {count} single-limb polynomials, seed 1",
+                                "batched_limb_polymul_per_s": count / sec, "ms_per_batch": sec * 1e3,
+                                "kernels_per_batch": kernels, "plain_limb_polymul_per_s": plain,
+                                "speedup_vs_plain": count / sec / plain}
+    del jobs
+    # ragged batch
+    inst = workloads.ragged_instances(512, seed=3)
+    rng = np.random.default_rng(3)
+    prim = {}
+    jobs, limbs_total, modmuls = [], 0, 0
+    for log_n, limbs in inst:
+        n = 1 << log_n
+        if n not in prim:
+            qq = workloads.ntt_primes(n, 16)
+            prim[n] = [(q, workloads.root_for(n, q), vk.NttTables(n, q, workloads.root_for(n, q))) for q in qq]
+        tq = prim[n][:limbs]
+        av = np.concatenate([workloads.uniform(rng, q, n) for q, _, _ in tq])
+        bv = np.concatenate([workloads.uniform(rng, q, n) for q, _, _ in tq])
+        jobs.append(([x[2] for x in tq], vk.Vector(ctx, av), vk.Vector(ctx, bv), vk.Vector(ctx, limbs * n)))
+        limbs_total += limbs
+        modmuls += limbs * modmuls_per_limb(n)
+        if len(jobs) == 1:
+            first = (av, bv, tq, n)
+    sec, kernels = batch_rate(vk, ctx, torch, jobs, reps=5)
+    av, bv, tq, n = first
+    ref, _ = orc.polymul(av[:n], bv[:n], n, tq[0][0], tq[0][1])
+    assert np.array_equal(jobs[0][3].download(n), ref), "ragged batch differs from the oracle"
+    out["ragged_batch"] = {"workload": "512 instances, n = 2^k with k uniform in 12..16, limbs uniform in 1..16, "
+                                       "seed 3", "limb_products": limbs_total, "ms_per_batch": sec * 1e3,
+                           "limb_polymul_per_s": limbs_total / sec, "gmodmul_per_s": modmuls / sec / 1e9,
+                           "kernels_per_batch": kernels}
+    del jobs
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -473,6 +554,7 @@ def main():
     }
     if rank == 0 and not args.no_serve:
         result["serving"] = serving_sweep(vk, torch)
+        result.update(extra_configs(vk, torch))
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline_sample(qs, ws, a_h, b_h)
     if rank == 0:

@@ -445,9 +445,9 @@ static int check_transform(const char *op, const struct vkhel_vector *a, const s
 				"%s: vectors of %" PRIu64 "/%" PRIu64 " words for n=%" PRIu64, op, a->length, res->length, t->n);
 	if (t->q >= ((uint64_t) 1 << 62) || t->q < 3)
 		return vkh_fail(res->ctx, VKHEL_ERR_UNSUPPORTED, "%s: q=%" PRIu64 " outside [3, 2^62)", op, t->q);
-	if (t->log_n > vkcu_max_fused_log_n() + 4)
+	if (t->log_n > vkcu_max_log_n())
 		return vkh_fail(res->ctx, VKHEL_ERR_UNSUPPORTED, "%s: n=%" PRIu64 " above 2^%u", op, t->n,
-				vkcu_max_fused_log_n() + 4);
+				vkcu_max_log_n());
 	if (t->n == 1)
 		return VKHEL_OK;
 	return vkh_devtab_get(res->ctx, t, d);

@@ -71,7 +71,7 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		const struct vkhel_ntt_tables *t = tables[k];
 		if (!t || t->n != n || n < 2)
 			return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: limb %u tables invalid", k);
-		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_fused_log_n() + 4)
+		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_log_n())
 			return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_add: limb %u (n, q) unsupported", k);
 	}
 	if (b->njobs + limbs > b->cap) {

@@ -110,8 +110,10 @@ int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,
 		uint32_t log_n, int sms);
 /* Integer-pipe microbenchmarks (peak.cu). */
 int vkcu_measure_int_peak(void *stream, int sms, double *bfly_per_s, double *imad_per_s);
-/* Largest log_n the fused single-launch kernels handle. */
+/* Largest log_n of the single-launch kernels (one CTA up to 2^14, one
+ * cluster up to 2^17), and the largest log_n handled at all (2^18). */
 uint32_t vkcu_max_fused_log_n(void);
+uint32_t vkcu_max_log_n(void);
 
 #ifdef __cplusplus
 }

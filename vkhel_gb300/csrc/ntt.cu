@@ -130,7 +130,9 @@ __global__ void k_inv_tail_global(const vkcu_ntt_job* __restrict__ jobs, int njo
   }
 }
 
-static constexpr int kMaxFused = 14;
+static constexpr int kMaxCta = 14;      // one CTA per transform
+static constexpr int kMaxCluster = 17;  // one cluster of up to 8 CTAs
+static constexpr int kMaxLogN = 18;     // one global pass + 2^14 sub-blocks
 
 static bool aligned32(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31) == 0; }
 
@@ -179,7 +181,8 @@ static int global_pass(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, con
 
 using namespace vk;
 
-extern "C" uint32_t vkcu_max_fused_log_n(void) { return kMaxFused; }
+extern "C" uint32_t vkcu_max_fused_log_n(void) { return kMaxCluster; }
+extern "C" uint32_t vkcu_max_log_n(void) { return kMaxLogN; }
 
 static bool jobs_aligned(const vkcu_ntt_job* jobs, const vkcu_ntt_job* one) {
   // Device job arrays are built by the library with aligned vectors; a single
@@ -191,27 +194,29 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
                                 uint32_t log_n, int sms) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
-  if (log_n < 1 || njobs < 1) return (int)cudaErrorInvalidValue;
-  if (log_n < 8 || (log_n <= (uint32_t)kMaxFused && !jobs_aligned(jobs, one)))
-    return simple(st, false, jobs, njobs, o, (int)log_n, sms);
-  if (log_n <= (uint32_t)kMaxFused) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms);
-  const int kk = (int)log_n - kMaxFused;
-  if (kk > 4) return (int)cudaErrorInvalidValue;
+  if (log_n < 1 || log_n > (uint32_t)kMaxLogN || njobs < 1) return (int)cudaErrorInvalidValue;
+  const bool aligned = jobs_aligned(jobs, one);
+  if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, false, jobs, njobs, o, (int)log_n, sms);
+  if (!aligned) return (int)cudaErrorMisalignedAddress;
+  if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms);
+  if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
+  const int kk = (int)log_n - kMaxCta;
   if (int e = global_pass<false>(st, jobs, njobs, o, (int)log_n, kk, sms)) return e;
-  return fwd_cta(st, jobs, njobs, o, kMaxFused, kk, sms);
+  return fwd_cta(st, jobs, njobs, o, kMaxCta, kk, sms);
 }
 
 extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
                                 uint32_t log_n, int sms) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
-  if (log_n < 1 || njobs < 1) return (int)cudaErrorInvalidValue;
-  if (log_n < 8 || (log_n <= (uint32_t)kMaxFused && !jobs_aligned(jobs, one)))
-    return simple(st, true, jobs, njobs, o, (int)log_n, sms);
-  if (log_n <= (uint32_t)kMaxFused) return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms);
-  const int kk = (int)log_n - kMaxFused;
-  if (kk > 4) return (int)cudaErrorInvalidValue;
-  if (int e = inv_cta(st, jobs, njobs, o, kMaxFused, kk, sms)) return e;
+  if (log_n < 1 || log_n > (uint32_t)kMaxLogN || njobs < 1) return (int)cudaErrorInvalidValue;
+  const bool aligned = jobs_aligned(jobs, one);
+  if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, true, jobs, njobs, o, (int)log_n, sms);
+  if (!aligned) return (int)cudaErrorMisalignedAddress;
+  if (log_n <= (uint32_t)kMaxCta) return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms);
+  if (log_n <= (uint32_t)kMaxCluster) return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
+  const int kk = (int)log_n - kMaxCta;
+  if (int e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms)) return e;
   return global_pass<true>(st, jobs, njobs, o, (int)log_n, kk, sms);
 }
 
@@ -219,8 +224,9 @@ extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, 
                             uint32_t log_n, int sms) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
-  if (log_n < 8 || log_n > (uint32_t)kMaxFused || njobs < 1) return (int)cudaErrorInvalidValue;
-  return poly_cta(st, jobs, njobs, o, (int)log_n, sms);
+  if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
+  if (log_n <= (uint32_t)kMaxCta) return poly_cta(st, jobs, njobs, o, (int)log_n, sms);
+  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
 }
 
 // Pointwise step of a composed polymul: c = c * scratch mod q over njobs

@@ -1,0 +1,260 @@
+// Transforms and fused polynomial multiply for n = 2^15 .. 2^17 on a thread-
+// block cluster of C = n / 2^14 CTAs with distributed shared memory (the
+// four-step decomposition):
+//
+//   forward:  column pass  -- the first log2 C stages act on columns
+//                             (words i, i + 2^14, ..., i + (C-1) 2^14); CTA r
+//                             reads its 2^14 / C columns from global memory,
+//                             runs the radix-C network in registers and writes
+//                             output j of every column into CTA j's shared
+//                             memory (DSMEM);
+//             row passes   -- each CTA then runs the remaining 14 stages on its
+//                             own 2^14-word sub-block, which is the contiguous
+//                             words [r 2^14, (r+1) 2^14) of the bit-reversed
+//                             output; the twiddle of local stage m' and local
+//                             block b is table[(C + r) m' + b];
+//   inverse:  row passes on each sub-block, then the column pass gathers every
+//             column from the C CTAs over DSMEM and runs the last log2 C
+//             stages with n^-1 folded in, writing global memory coalesced.
+//
+// Cluster barriers separate the phases: before a column pass writes another
+// CTA's shared memory (its owner has finished reading it), after it (the
+// sub-blocks are complete), and before the inverse gather.  Every CTA of a
+// cluster walks the same job sequence, and a final barrier keeps each CTA's
+// shared memory alive until the last remote read.
+#include <cooperative_groups.h>
+
+#include "ntt_core.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace vk {
+
+using SubShape = Shape<14, 32>;
+
+template <int LOGC>
+struct Cols {
+  static constexpr int C = 1 << LOGC, SUB = 1 << 14;
+  static constexpr int COLS = SUB >> LOGC;        // columns per CTA
+  static constexpr int PER = COLS / SubShape::T;  // columns per thread
+  static_assert(PER * C == SubShape::E, "a column pass moves E words per thread");
+  __device__ __forceinline__ static int col(int rank, int k) { return rank * COLS + (int)threadIdx.x + k * SubShape::T; }
+};
+
+// Forward column pass: global stages 0 .. LOGC-1 (exact first-stage rule),
+// outputs scattered to the owning CTAs' shared memory, lazy [0, 4q).
+template <int LOGC>
+__device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, const cg::cluster_group& cl, int rank,
+                                        const Tw& t) {
+  using K = Cols<LOGC>;
+  u64 v[K::PER * K::C];
+#pragma unroll
+  for (int k = 0; k < K::PER; k++)
+#pragma unroll
+    for (int j = 0; j < K::C; j++) v[k * K::C + j] = ld_stream(in + K::col(rank, k) + (size_t)j * K::SUB);
+  const ulonglong2 w0 = ld_tw(t.fwd + 1);
+  static_for<0, K::PER>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+#pragma unroll
+    for (int jj = 0; jj < K::C / 2; jj++) ct_first(v[k * K::C + jj], v[k * K::C + jj + K::C / 2], w0.x, w0.y, t);
+    ct_group<LOGC, 1, k * K::C>(v, t.fwd, 1u, t);
+  });
+#pragma unroll
+  for (int j = 0; j < K::C; j++) {
+    u64* rem = cl.map_shared_rank(sm, j);
+#pragma unroll
+    for (int k = 0; k < K::PER; k++) rem[pad(K::col(rank, k))] = v[k * K::C + j];
+  }
+}
+
+// Inverse column pass: gather, global stages LOGC-1 .. 0 with n^-1 folded in,
+// canonical words to global memory.
+template <int LOGC>
+__device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
+                                        const Tw& t) {
+  using K = Cols<LOGC>;
+  u64 v[K::PER * K::C];
+#pragma unroll
+  for (int j = 0; j < K::C; j++) {
+    const u64* rem = cl.map_shared_rank(sm, j);
+#pragma unroll
+    for (int k = 0; k < K::PER; k++) v[k * K::C + j] = rem[pad(K::col(rank, k))];
+  }
+  static_for<0, K::PER>([&](auto kc) {
+    constexpr int k = decltype(kc)::value;
+    gs_group<LOGC, k * K::C, false, true>(v, t.inv, 1u, t);
+  });
+#pragma unroll
+  for (int k = 0; k < K::PER; k++)
+#pragma unroll
+    for (int j = 0; j < K::C; j++) out[K::col(rank, k) + (size_t)j * K::SUB] = v[k * K::C + j];
+}
+
+template <int LOGC>
+__global__ void __launch_bounds__(512, 1)
+    k_ntt_fwd_cluster(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one) {
+  using S = SubShape;
+  using K = Cols<LOGC>;
+  extern __shared__ u64 sm[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int ncl = (int)gridDim.x / K::C, cid = (int)blockIdx.x / K::C;
+  const u32 tw_mult = (u32)(K::C + rank);
+#pragma unroll 1
+  for (int w = cid; w < njobs; w += ncl) {
+    const vkcu_ntt_job job = fetch_job(jobs, one, w);
+    const Tw t = load_tw(job.tw);
+    u64* out = reinterpret_cast<u64*>(job.out) + (size_t)rank * K::SUB;
+    cl.sync();
+    col_fwd<LOGC>(reinterpret_cast<const u64*>(job.in), sm, cl, rank, t);
+    cl.sync();
+    fwd_first_smem<S>(sm, t, tw_mult);
+    fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+      store16(v, out + 16 * g);
+    });
+  }
+  cl.sync();
+}
+
+template <int LOGC>
+__global__ void __launch_bounds__(512, 1)
+    k_ntt_inv_cluster(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one) {
+  using S = SubShape;
+  using K = Cols<LOGC>;
+  extern __shared__ u64 sm[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int ncl = (int)gridDim.x / K::C, cid = (int)blockIdx.x / K::C;
+  const u32 tw_mult = (u32)(K::C + rank);
+#pragma unroll 1
+  for (int w = cid; w < njobs; w += ncl) {
+    const vkcu_ntt_job job = fetch_job(jobs, one, w);
+    const Tw t = load_tw(job.tw);
+    const u64* in = reinterpret_cast<const u64*>(job.in) + (size_t)rank * K::SUB;
+    cl.sync();
+#pragma unroll 1
+    for (int i = 0; i < S::E / 16; i++) {
+      const int g = (int)threadIdx.x + i * S::T;
+      u64 v[16];
+      load16(v, in + 16 * g);
+      gs_group<4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+#pragma unroll
+      for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
+    }
+    __syncthreads();
+    inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
+    inv_last_smem<S>(sm, t, tw_mult);
+    cl.sync();
+    col_inv<LOGC>(reinterpret_cast<u64*>(job.out), sm, cl, rank, t);
+  }
+  cl.sync();
+}
+
+template <int LOGC>
+__global__ void __launch_bounds__(512, 1)
+    k_polymul_cluster(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one) {
+  using S = SubShape;
+  using K = Cols<LOGC>;
+  extern __shared__ u64 sm[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int ncl = (int)gridDim.x / K::C, cid = (int)blockIdx.x / K::C;
+  const u32 tw_mult = (u32)(K::C + rank);
+  constexpr unsigned kSlice = (unsigned)(K::COLS * 8);
+#pragma unroll 1
+  for (int w = cid; w < njobs; w += ncl) {
+    const vkcu_poly_job job = fetch_job(jobs, one, w);
+    const Tw t = load_tw(job.tw);
+    u64* scratch = reinterpret_cast<u64*>(job.scratch) + (size_t)rank * K::SUB;
+    if ((int)threadIdx.x < K::C)  // this CTA's column slices of a, for phase 1
+      prefetch_l2(reinterpret_cast<const u64*>(job.a) + (size_t)threadIdx.x * K::SUB + rank * K::COLS, kSlice);
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ph++) {
+      cl.sync();
+      col_fwd<LOGC>(reinterpret_cast<const u64*>(ph ? job.a : job.b), sm, cl, rank, t);
+      cl.sync();
+      fwd_first_smem<S>(sm, t, tw_mult);
+      fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
+        if (ph == 0) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+          store16(v, scratch + 16 * g);
+        } else {
+          u64 bh[16];
+          load16(bh, scratch + 16 * g);
+#pragma unroll
+          for (int j = 0; j < 16; j++)
+            sm[pad(16 * g + j)] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+        }
+      });
+    }
+    if (w + ncl < njobs && (int)threadIdx.x < K::C) {
+      const vkcu_poly_job nx = fetch_job(jobs, one, w + ncl);
+      prefetch_l2(reinterpret_cast<const u64*>(nx.b) + (size_t)threadIdx.x * K::SUB + rank * K::COLS, kSlice);
+    }
+    inv_passes<S>(sm, t, tw_mult, S::HEAD);
+    inv_last_smem<S>(sm, t, tw_mult);
+    cl.sync();
+    col_inv<LOGC>(reinterpret_cast<u64*>(job.c), sm, cl, rank, t);
+  }
+  cl.sync();
+}
+
+template <int LOGC, class Kern, class... Args>
+static int launch_cluster(Kern kern, cudaStream_t st, int njobs, Args... args) {
+  constexpr int C = 1 << LOGC;
+  static const int prepared = prepare(kern, SubShape::SMEM_BYTES);
+  if (prepared) return prepared;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(SubShape::T);
+  cfg.dynamicSmemBytes = SubShape::SMEM_BYTES;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cfg.gridDim = dim3(C);
+  int max_clusters = 0;
+  cudaError_t e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
+  if (e != cudaSuccess) return (int)e;
+  if (max_clusters < 1) return (int)cudaErrorInvalidConfiguration;
+  const int nclusters = njobs < max_clusters ? njobs : max_clusters;
+  cfg.gridDim = dim3(nclusters * C);
+  e = cudaLaunchKernelEx(&cfg, kern, args...);
+  vkcu_count_launches(1);
+  return (int)e;
+}
+
+int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc) {
+  switch (logc) {
+    case 1: return launch_cluster<1>(k_ntt_fwd_cluster<1>, st, njobs, jobs, njobs, one);
+    case 2: return launch_cluster<2>(k_ntt_fwd_cluster<2>, st, njobs, jobs, njobs, one);
+    case 3: return launch_cluster<3>(k_ntt_fwd_cluster<3>, st, njobs, jobs, njobs, one);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc) {
+  switch (logc) {
+    case 1: return launch_cluster<1>(k_ntt_inv_cluster<1>, st, njobs, jobs, njobs, one);
+    case 2: return launch_cluster<2>(k_ntt_inv_cluster<2>, st, njobs, jobs, njobs, one);
+    case 3: return launch_cluster<3>(k_ntt_inv_cluster<3>, st, njobs, jobs, njobs, one);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc) {
+  switch (logc) {
+    case 1: return launch_cluster<1>(k_polymul_cluster<1>, st, njobs, jobs, njobs, one);
+    case 2: return launch_cluster<2>(k_polymul_cluster<2>, st, njobs, jobs, njobs, one);
+    case 3: return launch_cluster<3>(k_polymul_cluster<3>, st, njobs, jobs, njobs, one);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace vk

@@ -273,6 +273,24 @@ __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, c
   __syncthreads();
 }
 
+// First forward pass on data already in shared memory (the sub-blocks of a
+// cluster transform): groups of 2^FIRSTK words, twiddle base tw_mult.
+template <class S>
+__device__ __forceinline__ void fwd_first_smem(u64* sm, const Tw& t, u32 tw_mult) {
+  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+#pragma unroll 1
+  for (int i = 0; i < G; i++) {
+    const int g = (int)threadIdx.x + i * S::T;
+    u64 v[1 << KK];
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];
+    ct_group<KK, 0, 0>(v, t.fwd, tw_mult, t);
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[j];
+  }
+  __syncthreads();
+}
+
 // Radix-16 forward passes s0 = FIRSTK, FIRSTK + 4, ..., HEAD on shared
 // memory.  The last pass hands each group (words 16g .. 16g+15) to epi(g, v)
 // instead of storing it back.  Ends with a barrier.
@@ -322,6 +340,24 @@ __device__ __forceinline__ void inv_passes(u64* sm, const Tw& t, u32 tw_mult, in
     }
     __syncthreads();
   }
+}
+
+// Last inverse pass of a cluster sub-block: stages FIRSTK-1 .. 0 in place in
+// shared memory, lazy [0, 2q), followed by a barrier.
+template <class S>
+__device__ __forceinline__ void inv_last_smem(u64* sm, const Tw& t, u32 tw_mult) {
+  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+#pragma unroll 1
+  for (int i = 0; i < G; i++) {
+    const int g = (int)threadIdx.x + i * S::T;
+    u64 v[1 << KK];
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];
+    gs_group<KK, 0, false, false>(v, t.inv, tw_mult, t);
+#pragma unroll
+    for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[j];
+  }
+  __syncthreads();
 }
 
 // Last inverse pass (stages FIRSTK-1 .. 0) from shared memory to `out`,
@@ -483,6 +519,10 @@ int fwd_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt
 int inv_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log,
             int sms);
 int poly_cta(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms);
+// cluster of 2^logc CTAs, n = 2^(14 + logc)
+int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
+int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc);
 
 template <class K>
 static int prepare(K kernel, int smem) {

@@ -365,7 +365,7 @@ int64_t vkhel_server_submit(struct vkhel_server *s, struct vkhel_ntt_tables *con
 		const struct vkhel_ntt_tables *t = tables[k];
 		if (!t || t->n != n || n < 2)
 			return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit: limb %u tables invalid", k);
-		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_fused_log_n() + 4)
+		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_log_n())
 			return -vkh_fail(NULL, VKHEL_ERR_UNSUPPORTED, "server_submit: limb %u (n, q) unsupported", k);
 	}
 	struct srv_req *r = calloc(1, sizeof(*r));
