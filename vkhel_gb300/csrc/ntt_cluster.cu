@@ -202,8 +202,10 @@ __global__ void __launch_bounds__(512, 1)
   cl.sync();
 }
 
-template <int LOGC, class Kern, class... Args>
-static int launch_cluster(Kern kern, cudaStream_t st, int njobs, Args... args) {
+// The kernel is a template argument so that each kernel gets its own
+// one-time attribute set-up (forward and inverse kernels share a signature).
+template <int LOGC, auto kern, class... Args>
+static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   constexpr int C = 1 << LOGC;
   static const int prepared = prepare(kern, SubShape::SMEM_BYTES);
   if (prepared) return prepared;
@@ -232,27 +234,27 @@ static int launch_cluster(Kern kern, cudaStream_t st, int njobs, Args... args) {
 
 int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc) {
   switch (logc) {
-    case 1: return launch_cluster<1>(k_ntt_fwd_cluster<1>, st, njobs, jobs, njobs, one);
-    case 2: return launch_cluster<2>(k_ntt_fwd_cluster<2>, st, njobs, jobs, njobs, one);
-    case 3: return launch_cluster<3>(k_ntt_fwd_cluster<3>, st, njobs, jobs, njobs, one);
+    case 1: return launch_cluster<1, k_ntt_fwd_cluster<1>>(st, njobs, jobs, njobs, one);
+    case 2: return launch_cluster<2, k_ntt_fwd_cluster<2>>(st, njobs, jobs, njobs, one);
+    case 3: return launch_cluster<3, k_ntt_fwd_cluster<3>>(st, njobs, jobs, njobs, one);
     default: return (int)cudaErrorInvalidValue;
   }
 }
 
 int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc) {
   switch (logc) {
-    case 1: return launch_cluster<1>(k_ntt_inv_cluster<1>, st, njobs, jobs, njobs, one);
-    case 2: return launch_cluster<2>(k_ntt_inv_cluster<2>, st, njobs, jobs, njobs, one);
-    case 3: return launch_cluster<3>(k_ntt_inv_cluster<3>, st, njobs, jobs, njobs, one);
+    case 1: return launch_cluster<1, k_ntt_inv_cluster<1>>(st, njobs, jobs, njobs, one);
+    case 2: return launch_cluster<2, k_ntt_inv_cluster<2>>(st, njobs, jobs, njobs, one);
+    case 3: return launch_cluster<3, k_ntt_inv_cluster<3>>(st, njobs, jobs, njobs, one);
     default: return (int)cudaErrorInvalidValue;
   }
 }
 
 int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc) {
   switch (logc) {
-    case 1: return launch_cluster<1>(k_polymul_cluster<1>, st, njobs, jobs, njobs, one);
-    case 2: return launch_cluster<2>(k_polymul_cluster<2>, st, njobs, jobs, njobs, one);
-    case 3: return launch_cluster<3>(k_polymul_cluster<3>, st, njobs, jobs, njobs, one);
+    case 1: return launch_cluster<1, k_polymul_cluster<1>>(st, njobs, jobs, njobs, one);
+    case 2: return launch_cluster<2, k_polymul_cluster<2>>(st, njobs, jobs, njobs, one);
+    case 3: return launch_cluster<3, k_polymul_cluster<3>>(st, njobs, jobs, njobs, one);
     default: return (int)cudaErrorInvalidValue;
   }
 }
