@@ -139,6 +139,23 @@ uint32_t vkhel_batch_jobs(const struct vkhel_batch *batch);
 uint32_t vkhel_batch_kernels(const struct vkhel_batch *batch);
 void vkhel_batch_destroy(struct vkhel_batch *batch);
 
+/* ---- kernel variants (autotuning) ----
+ * Each fused kernel family has, per degree 2^log_n, a few compiled variants
+ * (threads per polynomial, radix-16 groups in flight per thread); the table
+ * of which one to launch is read once per process from $VKHEL_TUNE_TABLE or
+ * from tuning/gb300.txt beside the package (written by vkhel_gb300.autotune).
+ * Family VKHEL_TUNE_BATCH, log_n 0: 1 = run the degree classes of a batch on
+ * concurrent streams. */
+enum vkhel_tune_family {
+	VKHEL_TUNE_POLYMUL = 0,
+	VKHEL_TUNE_FORWARD = 1,
+	VKHEL_TUNE_INVERSE = 2,
+	VKHEL_TUNE_BATCH = 3
+};
+int vkhel_tune_set(uint32_t family, uint32_t log_n, int32_t variant);
+int vkhel_tune_get(uint32_t family, uint32_t log_n);
+int vkhel_tune_load(const char *path);
+
 /* ---- serving: continuous batching of polynomial-multiply requests ----
  * A server owns a private context (device VKHEL_DEVICE), three streams and a
  * scheduler thread.  Requests (limbs limb products of one degree with host

@@ -81,6 +81,9 @@ _SIGNATURES = [
     ("vkhel_batch_jobs", u32, [vp]),
     ("vkhel_batch_kernels", u32, [vp]),
     ("vkhel_batch_destroy", None, [vp]),
+    ("vkhel_tune_set", ctypes.c_int, [u32, u32, ctypes.c_int32]),
+    ("vkhel_tune_get", ctypes.c_int, [u32, u32]),
+    ("vkhel_tune_load", ctypes.c_int, [ctypes.c_char_p]),
     ("vkhel_server_create", vp, [vp]),
     ("vkhel_server_submit", ctypes.c_int64, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_server_wait", ctypes.c_int, [vp, ctypes.c_int64, u32]),

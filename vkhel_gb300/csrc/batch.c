@@ -42,6 +42,12 @@ struct vkhel_batch {
 	vkcu_ntt_job *dev_ntt; /* [3 * njobs]: b->scratch, a->c, c->c */
 	void *graph;
 	uint32_t kernels;
+	/* concurrent degree classes: one stream and one join event per class
+	 * after the first, one fork event */
+	uint32_t naux;
+	void *aux[MAX_CLASSES];
+	void *join[MAX_CLASSES];
+	void *fork;
 };
 
 struct vkhel_batch *vkhel_batch_create(struct vkhel_ctx *ctx) {
@@ -177,7 +183,32 @@ void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struc
 	}
 }
 
+/* Same, with class k > 0 on aux[k - 1]: the auxiliary streams wait for
+ * `fork` recorded on `stream`, and `stream` waits for each join[k - 1], so
+ * the classes run concurrently and the whole still ends on `stream` (this is
+ * also how a CUDA graph capture picks up the parallel branches). */
+int vkh_issue_classes_forked(void *stream, void *const *aux, void *fork, void *const *join, int sms,
+		const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt, const struct vkh_job_class *classes,
+		uint32_t nclasses) {
+	if (nclasses < 2)
+		return vkh_issue_classes(stream, sms, dev_poly, dev_ntt, classes, nclasses);
+	int e = vkcu_event_record(fork, stream);
+	for (uint32_t k = 1; !e && k < nclasses; k++)
+		e = vkcu_stream_wait(aux[k - 1], fork);
+	for (uint32_t k = 0; !e && k < nclasses; k++)
+		e = vkh_issue_classes(k ? aux[k - 1] : stream, sms, dev_poly, dev_ntt, &classes[k], 1);
+	for (uint32_t k = 1; !e && k < nclasses; k++) {
+		e = vkcu_event_record(join[k - 1], aux[k - 1]);
+		if (!e)
+			e = vkcu_stream_wait(stream, join[k - 1]);
+	}
+	return e;
+}
+
 static int issue(struct vkhel_batch *b) {
+	if (b->naux)
+		return vkh_issue_classes_forked(b->ctx->stream, b->aux, b->fork, b->join, b->ctx->sms, b->dev_poly,
+				b->dev_ntt, b->classes, b->nclasses);
 	return vkh_issue_classes(b->ctx->stream, b->ctx->sms, b->dev_poly, b->dev_ntt, b->classes, b->nclasses);
 }
 
@@ -251,6 +282,18 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	b->dev_poly = b->dev;
 	b->dev_ntt = (vkcu_ntt_job *) ((char *) b->dev + ntt_off);
 
+	if (b->nclasses > 1 && vkh_variant(3, 0) == 1) {
+		e = vkcu_event_create(&b->fork);
+		for (uint32_t k = 0; !e && k + 1 < b->nclasses; k++) {
+			e = vkcu_stream_create(&b->aux[k]);
+			if (!e)
+				e = vkcu_event_create(&b->join[k]);
+			if (!e)
+				b->naux = k + 1;
+		}
+		if (e)
+			return vkh_cuda(ctx, e, "batch_commit: class streams");
+	}
 	const uint64_t before = vkcu_launch_count();
 	if (flags & VKHEL_BATCH_GRAPH) {
 		e = vkcu_capture_begin(ctx->stream);
@@ -307,6 +350,11 @@ void vkhel_batch_destroy(struct vkhel_batch *b) {
 	struct vkhel_ctx *ctx = b->ctx;
 	vkcu_sync(ctx->stream);
 	vkcu_graph_destroy(b->graph);
+	for (uint32_t k = 0; k < b->naux; k++) {
+		vkcu_stream_destroy(b->aux[k]);
+		vkcu_event_destroy(b->join[k]);
+	}
+	vkcu_event_destroy(b->fork);
 	vkh_dev_free(ctx, b->dev, b->dev_bytes);
 	vkh_dev_free(ctx, b->scratch, b->scratch_bytes);
 	free(b->recs);

@@ -89,8 +89,13 @@ struct vkh_job_class {
 };
 int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt,
 		const struct vkh_job_class *classes, uint32_t nclasses);
+int vkh_issue_classes_forked(void *stream, void *const *aux, void *fork, void *const *join, int sms,
+		const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt, const struct vkh_job_class *classes,
+		uint32_t nclasses);
 void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struct vkh_job_class *classes,
 		uint32_t nclasses);
+/* tuning.c -- variant of kernel family (VKHEL_TUNE_*) for degree 2^log_n */
+int vkh_variant(int family, int log_n);
 /* Lookup only: NULL when (n, q, w) has no device copy in ctx yet. */
 const struct vkh_devtab *vkh_devtab_find(const struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t);
 

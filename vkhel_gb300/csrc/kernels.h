@@ -108,6 +108,9 @@ int vkcu_polymul(void *stream, const vkcu_poly_job *jobs, int njobs,
  * output) for every job: the pointwise step of a polymul that is not fused. */
 int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,
 		uint32_t log_n, int sms);
+/* Kernel variant table (tuning.c): family 0 = fused polymul, 1 = forward,
+ * 2 = inverse, 3 = batch options. */
+int vkh_variant(int family, int log_n);
 /* Integer-pipe microbenchmarks (peak.cu). */
 int vkcu_measure_int_peak(void *stream, int sms, double *bfly_per_s, double *imad_per_s);
 /* Largest log_n of the single-launch kernels (one CTA up to 2^14, one

@@ -198,11 +198,11 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
   const bool aligned = jobs_aligned(jobs, one);
   if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, false, jobs, njobs, o, (int)log_n, sms);
   if (!aligned) return (int)cudaErrorMisalignedAddress;
-  if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms);
+  if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(1, (int)log_n));
   if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
   const int kk = (int)log_n - kMaxCta;
   if (int e = global_pass<false>(st, jobs, njobs, o, (int)log_n, kk, sms)) return e;
-  return fwd_cta(st, jobs, njobs, o, kMaxCta, kk, sms);
+  return fwd_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(1, kMaxCta));
 }
 
 extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
@@ -213,10 +213,10 @@ extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njob
   const bool aligned = jobs_aligned(jobs, one);
   if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, true, jobs, njobs, o, (int)log_n, sms);
   if (!aligned) return (int)cudaErrorMisalignedAddress;
-  if (log_n <= (uint32_t)kMaxCta) return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms);
+  if (log_n <= (uint32_t)kMaxCta) return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(2, (int)log_n));
   if (log_n <= (uint32_t)kMaxCluster) return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
   const int kk = (int)log_n - kMaxCta;
-  if (int e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms)) return e;
+  if (int e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(2, kMaxCta))) return e;
   return global_pass<true>(st, jobs, njobs, o, (int)log_n, kk, sms);
 }
 
@@ -225,7 +225,7 @@ extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, 
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
   if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
-  if (log_n <= (uint32_t)kMaxCta) return poly_cta(st, jobs, njobs, o, (int)log_n, sms);
+  if (log_n <= (uint32_t)kMaxCta) return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
   return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
 }
 

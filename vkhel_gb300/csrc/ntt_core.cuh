@@ -225,9 +225,10 @@ __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32
 // a direction share one loop body (the stage offset is a runtime value), and
 // the fused polymul runs its two forward transforms through the same code.
 
-template <int LOGN_, int E_>
+template <int LOGN_, int E_, int U_ = 1>
 struct Shape {
   static constexpr int LOGN = LOGN_, E = E_;
+  static constexpr int U = U_;  // radix-16 groups of a thread in flight at once (1 or 2)
   static constexpr int N = 1 << LOGN, T = N / E;
   static constexpr int HEAD = LOGN - 4;  // first stage of the last pass
   static constexpr int FIRSTK = HEAD % 4 == 0 ? 4 : HEAD % 4;
@@ -300,7 +301,7 @@ __device__ __forceinline__ void fwd_passes(u64* sm, const Tw& t, u32 tw_mult, Ep
   for (int s0 = S::FIRSTK; s0 <= S::HEAD; s0 += 4) {
     const Pass16 ps(S::LOGN, s0, tw_mult);
     const int st = 1 << ps.lt;
-#pragma unroll 1
+#pragma unroll(S::U)
     for (int i = 0; i < S::E / 16; i++) {
       const int g = (int)threadIdx.x + i * S::T;
       const int a0 = ps.first(g);
@@ -327,7 +328,7 @@ __device__ __forceinline__ void inv_passes(u64* sm, const Tw& t, u32 tw_mult, in
   for (int s0 = s_top; s0 >= S::FIRSTK; s0 -= 4) {
     const Pass16 ps(S::LOGN, s0, tw_mult);
     const int st = 1 << ps.lt;
-#pragma unroll 1
+#pragma unroll(S::U)
     for (int i = 0; i < S::E / 16; i++) {
       const int g = (int)threadIdx.x + i * S::T;
       const int a0 = ps.first(g);
@@ -413,10 +414,10 @@ __device__ __forceinline__ J fetch_job(const J* jobs, const J& one, int jid) {
 // (transforms of 2^(LOGN + sub_log) words after / before the global passes),
 // sub-block `sub` using twiddle multiplier 2^sub_log + sub.
 
-template <int LOGN, int E>
+template <int LOGN, int E, int U>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     k_ntt_fwd(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log) {
-  using S = Shape<LOGN, E>;
+  using S = Shape<LOGN, E, U>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
 #pragma unroll 1
@@ -436,10 +437,10 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
   }
 }
 
-template <int LOGN, int E>
+template <int LOGN, int E, int U>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     k_ntt_inv(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log) {
-  using S = Shape<LOGN, E>;
+  using S = Shape<LOGN, E, U>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
 #pragma unroll 1
@@ -472,10 +473,10 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
 // last pass multiplies by NTT(b) (read back at the words this thread wrote)
 // into shared memory; the inverse transform then writes c.  a is prefetched
 // into L2 while b is transformed, the next job's b while a is.
-template <int LOGN, int E>
+template <int LOGN, int E, int U>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one) {
-  using S = Shape<LOGN, E>;
+  using S = Shape<LOGN, E, U>;
   extern __shared__ u64 sm[];
   constexpr unsigned kChunk = (unsigned)(S::N * 8 / 4);
 #pragma unroll 1
@@ -514,11 +515,14 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
 // ---------------------------------------------------------------------------
 // Host side: per-family launchers (one translation unit each).
 
+// variant: 0 = default shape, 1 = two radix-16 groups per thread in flight,
+// 2 = the other words-per-thread shape (2^10..2^13 only); others -> 0.
 int fwd_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log,
-            int sms);
+            int sms, int variant);
 int inv_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log,
-            int sms);
-int poly_cta(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms);
+            int sms, int variant);
+int poly_cta(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
+             int variant);
 // cluster of 2^logc CTAs, n = 2^(14 + logc)
 int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
 int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
@@ -538,17 +542,30 @@ static int grid_for(K kernel, int threads, int smem, long work, int sms) {
   return (int)(work < cap ? work : cap);
 }
 
-// Elements per thread for each fused degree.
-#define VK_FOR_LOGN(X)                          \
-  switch (log_n) {                              \
-    case 8: return X(8, 16);                    \
-    case 9: return X(9, 16);                    \
-    case 10: return X(10, 16);                  \
-    case 11: return X(11, 16);                  \
-    case 12: return X(12, 16);                  \
-    case 13: return X(13, 32);                  \
-    case 14: return X(14, 32);                  \
-    default: return (int)cudaErrorInvalidValue; \
+// Shapes per degree and variant: words per thread E and group unroll U.
+#define VK_FOR_LOGN(X)                                                        \
+  switch (log_n * 4 + (variant == 1 ? 1 : variant == 2 ? 2 : 0)) {            \
+    case 8 * 4: return X(8, 16, 1);                                           \
+    case 8 * 4 + 1: return X(8, 16, 2);                                       \
+    case 9 * 4: return X(9, 16, 1);                                           \
+    case 9 * 4 + 1: return X(9, 16, 2);                                       \
+    case 10 * 4: return X(10, 16, 1);                                         \
+    case 10 * 4 + 1: return X(10, 16, 2);                                     \
+    case 10 * 4 + 2: return X(10, 32, 1);                                     \
+    case 11 * 4: return X(11, 16, 1);                                         \
+    case 11 * 4 + 1: return X(11, 16, 2);                                     \
+    case 11 * 4 + 2: return X(11, 32, 1);                                     \
+    case 12 * 4: return X(12, 16, 1);                                         \
+    case 12 * 4 + 1: return X(12, 16, 2);                                     \
+    case 12 * 4 + 2: return X(12, 32, 1);                                     \
+    case 13 * 4: return X(13, 32, 1);                                         \
+    case 13 * 4 + 1: return X(13, 32, 2);                                     \
+    case 13 * 4 + 2: return X(13, 16, 1);                                     \
+    case 14 * 4: return X(14, 32, 1);                                         \
+    case 14 * 4 + 1: return X(14, 32, 2);                                     \
+    default:                                                                  \
+      if (variant != 0) { variant = 0; goto retry; }                          \
+      return (int)cudaErrorInvalidValue;                                      \
   }
 
 }  // namespace vk

@@ -5,10 +5,10 @@
 
 namespace vk {
 
-template <int LOGN, int E>
+template <int LOGN, int E, int U>
 static int launch(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int sub_log, int sms) {
-  using S = Shape<LOGN, E>;
-  auto kern = k_ntt_fwd<LOGN, E>;
+  using S = Shape<LOGN, E, U>;
+  auto kern = k_ntt_fwd<LOGN, E, U>;
   static const int prepared = prepare(kern, S::SMEM_BYTES);
   if (prepared) return prepared;
   const int grid = grid_for(kern, S::T, S::SMEM_BYTES, (long)njobs << sub_log, sms);
@@ -17,8 +17,10 @@ static int launch(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vk
   return (int)cudaGetLastError();
 }
 
-int fwd_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log, int sms) {
-#define X(L, E) launch<L, E>(st, jobs, njobs, one, sub_log, sms)
+int fwd_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sub_log, int sms,
+            int variant) {
+retry:
+#define X(L, E, U) launch<L, E, U>(st, jobs, njobs, one, sub_log, sms)
   VK_FOR_LOGN(X)
 #undef X
 }

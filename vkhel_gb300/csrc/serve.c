@@ -60,6 +60,9 @@ struct srv_slot {
 struct vkhel_server {
 	struct vkhel_ctx *ctx; /* private context: tables cache, pool, SM count */
 	void *s_in, *s_comp, *s_out;
+	/* concurrent degree classes of a micro-batch (tuning flag) */
+	int forked;
+	void *aux[SRV_MAX_CLASSES], *join[SRV_MAX_CLASSES], *fork;
 	uint64_t budget, bytes;
 	uint32_t max_limbs, nslots;
 	struct srv_slot *slots;
@@ -165,7 +168,9 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 		if (!e)
 			e = vkcu_stream_wait(s->s_comp, sl->ev_in);
 		if (!e)
-			e = vkh_issue_classes(s->s_comp, ctx->sms, dpoly, dntt, classes, nclasses);
+			e = s->forked ? vkh_issue_classes_forked(s->s_comp, s->aux, s->fork, s->join, ctx->sms, dpoly, dntt,
+					classes, nclasses)
+				: vkh_issue_classes(s->s_comp, ctx->sms, dpoly, dntt, classes, nclasses);
 		if (!e)
 			e = vkcu_event_record(sl->ev_comp, s->s_comp);
 		if (!e)
@@ -315,6 +320,14 @@ struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg) 
 		e = vkcu_stream_create(&s->s_comp);
 	if (!e)
 		e = vkcu_stream_create(&s->s_out);
+	s->forked = vkh_variant(3, 0) == 1;
+	if (!e && s->forked)
+		e = vkcu_event_create(&s->fork);
+	for (uint32_t k = 0; !e && s->forked && k < SRV_MAX_CLASSES; k++) {
+		e = vkcu_stream_create(&s->aux[k]);
+		if (!e)
+			e = vkcu_event_create(&s->join[k]);
+	}
 	const uint64_t cap = (uint64_t) s->max_limbs + 64;
 	for (uint32_t k = 0; !e && k < s->nslots; k++) {
 		struct srv_slot *sl = &s->slots[k];
@@ -529,6 +542,14 @@ void vkhel_server_destroy(struct vkhel_server *s) {
 	for (int i = 0; i < 3; i++)
 		if (streams[i])
 			vkcu_stream_destroy(streams[i]);
+	for (int k = 0; k < SRV_MAX_CLASSES; k++) {
+		if (s->aux[k]) {
+			vkcu_sync(s->aux[k]);
+			vkcu_stream_destroy(s->aux[k]);
+		}
+		vkcu_event_destroy(s->join[k]);
+	}
+	vkcu_event_destroy(s->fork);
 	for (int64_t i = 0; i + 1 < s->next_id; i++) {
 		if (s->by_id[i]) {
 			free(s->by_id[i]->tables);
