@@ -362,7 +362,8 @@ def main():
     # the first wave of the next, as in a continuous stream of batches.
     ctxs = [vk.Context(), vk.Context()]
     streams = [torch.cuda.ExternalStream(c.stream) for c in ctxs]
-    qs, ws, a_h, b_h = workloads.rns_batch(N, LIMBS, PAIRS, SEED + 1000 * rank)
+    from vkhel_gb300 import replicas
+    qs, ws, a_h, b_h = workloads.rns_batch(N, LIMBS, PAIRS, replicas.rank_seed(SEED, rank))
     tabs = [[vk.NttTables(N, q, w) for q, w in zip(qs, ws)] for _ in ctxs]
     words = PAIRS * LIMBS * N
     stride = LIMBS * N
@@ -434,13 +435,10 @@ def main():
     launches = vk.launch_count() - launches0
     total_ms = max(t_start.elapsed_time(e) for e in t_end)
     clk = clocks.stop()
+    units, total_s, value = replicas.aggregate(total_ms * 1e-3, PAIRS * LIMBS * args.steps)
+    total_ms = total_s * 1e3
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
-    units = PAIRS * LIMBS * args.steps * world
-    value = units / (total_ms * 1e-3)
     eff_ms = total_ms / args.steps
 
     # ---- roofline of the fused kernel ----
@@ -503,7 +501,26 @@ def main():
         for l in range(LIMBS):
             ref, _ = orc.polymul(a_h[0, l], b_h[0, l], N, qs[l], ws[l])
             assert np.array_equal(out[l * N:(l + 1) * N], ref), "bench e2e: result differs from the oracle"
+    # raw pinned-copy bandwidth through the same API, for reading the e2e number
+    def copy_rate(fn, reps=8):
+        fn()
+        for c in ctxs:
+            c.sync()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        for c in ctxs:
+            c.sync()
+        return (time.perf_counter() - t) / reps
+    va0, vc1 = e2e_sets[0][1], e2e_sets[1][3]
+    h2d_s = copy_rate(lambda: L.vkhel_vector_upload_async(va0.ptr, pins[0][0].data_ptr(), words))
+    d2h_s = copy_rate(lambda: L.vkhel_vector_download_async(vc1.ptr, pins[1][2].data_ptr(), words))
+    both_s = copy_rate(lambda: (L.vkhel_vector_upload_async(va0.ptr, pins[0][0].data_ptr(), words),
+                                L.vkhel_vector_download_async(vc1.ptr, pins[1][2].data_ptr(), words)))
+    copy_gbps = {"h2d": 8 * words / h2d_s / 1e9, "d2h": 8 * words / d2h_s / 1e9,
+                 "h2d_and_d2h_concurrent": 2 * 8 * words / both_s / 1e9, "bytes_per_copy": 8 * words}
     e2e = {"value": PAIRS * LIMBS * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * words,
+           "copy_gbps": copy_gbps,
            "d2h_bytes_per_step": 8 * words, "ms_per_step": e2e_s * 1e3,
            "path": "vkhel_vector_upload_async x2 + vkhel_batch_launch + vkhel_vector_download_async, "
                    "pinned host buffers, two contexts pipelined, host wall clock"}

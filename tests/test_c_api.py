@@ -1,0 +1,72 @@
+"""The public C header and libvkhel.so as a C program sees them.
+
+tests/c/test_vkhel_api.c includes only include/vkhel/vkhel.h and replays the
+reference's golden operations with the reference test program's call
+pattern.  On a CPU-only machine it must compile, link against libvkhel.so and
+report the missing device cleanly (exit 77); on the GPU every case must match.
+"""
+import os
+import subprocess
+
+import pytest
+
+from conftest import ROOT, load_golden
+
+SRC = os.path.join(ROOT, "tests", "c", "test_vkhel_api.c")
+
+
+def _build(tmp_path):
+    from vkhel_gb300 import LIB_PATH
+    exe = str(tmp_path / "test_vkhel_api")
+    libdir = os.path.dirname(LIB_PATH)
+    subprocess.run(["gcc", "-std=gnu11", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include", "vkhel"),
+                    SRC, "-o", exe, "-L", libdir, "-lvkhel", f"-Wl,-rpath,{libdir}"], check=True)
+    cases = tmp_path / "cases.txt"
+    lines = []
+    for op in load_golden("reference_vectors.json")["ops"]:
+        p = op["params"]
+        name = op["op"]
+        if name in ("forward_transform", "inverse_transform"):
+            params = [p["n"], p["q"], p["w"]]
+        elif name == "elemfma":
+            params = [p["multiplier"], p["mod"], "0"]
+        elif name == "elemmul":
+            params = [p["mod"], "0", "0"]
+        elif name == "elemmod":
+            params = [p["mod"], p["q"], "0"]
+        elif name == "elemgtadd":
+            params = [p["bound"], p["diff"], "0"]
+        elif name == "elemgtsub":
+            params = [p["bound"], p["diff"], p["mod"]]
+        else:
+            params = ["0", "0", "0"]
+        lines.append(" ".join([name] + params))
+        lines.append(" ".join(["a", str(len(op["a"]))] + op["a"]))
+        if "b" in op:
+            lines.append(" ".join(["b", str(len(op["b"]))] + op["b"]))
+        lines.append(" ".join(["e", str(len(op["expected"]))] + op["expected"]))
+    cases.write_text("\n".join(lines) + "\n")
+    return exe, str(cases)
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_c_program_links_and_reports_no_device(vk, tmp_path):
+    exe, cases = _build(tmp_path)
+    r = subprocess.run([exe, cases], capture_output=True, text=True)
+    assert r.returncode == 77 and "no CUDA device" in r.stdout
+
+
+@pytest.mark.gpu
+def test_c_program_replays_reference_golden_vectors(vk, tmp_path):
+    exe, cases = _build(tmp_path)
+    r = subprocess.run([exe, cases], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "35 cases, 0 failed" in r.stdout
