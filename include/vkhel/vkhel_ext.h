@@ -77,6 +77,11 @@ int vkhel_ntt_tables_copy(const struct vkhel_ntt_tables *t, uint64_t *roots,
 		uint64_t *inv_roots, uint64_t *roots_shoup, uint64_t *inv_roots_shoup);
 /* Reference: src/ntt_tables.c:46-63. */
 void vkhel_ntt_tables_dbgprint(struct vkhel_ntt_tables *t);
+/* Copy the context's device copy of the tables out (making it resident
+ * first); equal to vkhel_ntt_tables_copy word for word. */
+int vkhel_ntt_tables_device_copy(struct vkhel_ctx *ctx,
+		const struct vkhel_ntt_tables *t, uint64_t *roots, uint64_t *inv_roots,
+		uint64_t *roots_shoup, uint64_t *inv_roots_shoup);
 
 /* ---- arithmetic ---- */
 /* (a * multiplier + b) mod `mod`, canonical, for every 64-bit input: what

@@ -69,6 +69,7 @@ _SIGNATURES = [
     ("vkhel_vector_dbgprint", None, [vp]),
     ("vkhel_ntt_tables_copy", ctypes.c_int, [vp, vp, vp, vp, vp]),
     ("vkhel_ntt_tables_dbgprint", None, [vp]),
+    ("vkhel_ntt_tables_device_copy", ctypes.c_int, [vp, vp, vp, vp, vp, vp]),
     ("vkhel_vector_elemfma_canonical", None, [vp, vp, vp, u64, u64]),
     ("vkhel_vector_polymul", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_vector_polymul_noalloc", ctypes.c_int, [vp, vp, vp, vp]),
@@ -235,6 +236,12 @@ class NttTables:
     def arrays(self):
         out = [np.zeros(self.n, dtype=np.uint64) for _ in range(4)]
         lib().vkhel_ntt_tables_copy(self.ptr, *[o.ctypes.data for o in out])
+        return dict(zip(("roots", "inv_roots", "roots_shoup", "inv_roots_shoup"), out))
+
+    def device_arrays(self, ctx):
+        """The context's device copy (generated on the GPU when q < 2^61)."""
+        out = [np.zeros(self.n, dtype=np.uint64) for _ in range(4)]
+        _status(ctx.ptr, lib().vkhel_ntt_tables_device_copy(ctx.ptr, self.ptr, *[o.ctypes.data for o in out]))
         return dict(zip(("roots", "inv_roots", "roots_shoup", "inv_roots_shoup"), out))
 
     def close(self):

@@ -178,3 +178,51 @@ extern "C" int vkcu_elemmodbytwo(void* stream, uint64_t* res, const uint64_t* a,
                                  uint64_t signed_bound) {
   return launch(stream, res, a, nullptr, len, OpModTwo{signed_bound});
 }
+
+// ---------------------------------------------------------------------------
+// Twiddle tables generated on the device for one (n, q, w) with q < 2^61 and
+// w^n = -1.  Word i of the power sequence is w^i = phi[i >> lb] * plo[i & mask]
+// (exact Barrett product of two canonical powers, so equal to the reference's
+// sequential products); it goes to slot bitrev(i) of the forward table, and
+// q - w^i to slot bitrev(n - i) of the inverse table (w^-(n-i) = -w^i).  Each
+// entry is stored with its Shoup factor floor(r 2^64 / q).
+namespace vk {
+
+__device__ __forceinline__ u64 shoup_factor(u64 r, u64 q) {
+  return (u64)((((unsigned __int128)r) << 64) / q);
+}
+
+__global__ void k_twiddles(u64* __restrict__ fwd, u64* __restrict__ inv, const u64* __restrict__ phi,
+                           const u64* __restrict__ plo, u32 log_n, u32 lb, u64 q, u64 mu, u32 qbits) {
+  const u64 n = 1ull << log_n;
+  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+    const u64 x = phi[i >> lb], y = plo[i & ((1ull << lb) - 1)];
+    const u64 p = i == 0 ? 1ull : ref_reduce128(mulhi(x, y), x * y, q, mu, qbits);
+    const u32 s = __brev((u32)i) >> (32 - log_n);
+    fwd[2 * s] = p;
+    fwd[2 * s + 1] = shoup_factor(p, q);
+    if (i == 0) {
+      inv[0] = 1;
+      inv[1] = shoup_factor(1, q);
+    } else {
+      const u32 s2 = __brev((u32)(n - i)) >> (32 - log_n);
+      inv[2 * s2] = q - p;
+      inv[2 * s2 + 1] = shoup_factor(q - p, q);
+    }
+  }
+}
+
+}  // namespace vk
+
+extern "C" int vkcu_twiddles(void* stream, uint64_t* fwd, uint64_t* inv, const uint64_t* phi, const uint64_t* plo,
+                             uint32_t log_n, uint32_t lb, uint64_t q, uint64_t mu, uint32_t qbits) {
+  if (log_n < 1 || log_n > 31) return (int)cudaErrorInvalidValue;
+  const uint64_t n = 1ull << log_n;
+  uint64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  vk::k_twiddles<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<vk::u64*>(fwd), reinterpret_cast<vk::u64*>(inv), reinterpret_cast<const vk::u64*>(phi),
+      reinterpret_cast<const vk::u64*>(plo), log_n, lb, q, mu, qbits);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
+}

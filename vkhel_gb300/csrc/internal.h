@@ -56,8 +56,13 @@ struct vkhel_vector {
 struct vkhel_ntt_tables {
 	uint64_t n, q, w;
 	uint32_t log_n;
-	/* host arrays, the reference's layout (include/priv/ntt_tables.h:6-15) */
+	/* host arrays, the reference's layout (include/priv/ntt_tables.h:6-15);
+	 * computed on first use when the device can generate the tables */
 	uint64_t *roots, *inv_roots, *roots_shoup, *inv_roots_shoup;
+	int host_ready;
+	/* q < 2^61, n >= 2 and w^n = -1: generated on the device */
+	int device_gen;
+	uint64_t w_red; /* w mod q */
 	/* derived constants for the device twiddle set */
 	uint64_t mu, ninv, ninv_s, w1ninv, w1ninv_s;
 	uint32_t qbits;

@@ -94,6 +94,11 @@ int vkcu_elemgtadd(void *stream, uint64_t *res, const uint64_t *a,
 int vkcu_elemmodbytwo(void *stream, uint64_t *res, const uint64_t *a,
 		uint64_t len, uint64_t signed_bound);
 
+/* Device twiddle generation (q < 2^61, w^n = -1): fwd/inv are n interleaved
+ * (root, shoup) pairs; phi[j] = w^(j 2^lb), plo[k] = w^k for k < 2^lb. */
+int vkcu_twiddles(void *stream, uint64_t *fwd, uint64_t *inv, const uint64_t *phi,
+		const uint64_t *plo, uint32_t log_n, uint32_t lb, uint64_t q, uint64_t mu, uint32_t qbits);
+
 /* ---- transforms (ntt.cu) ----
  * `jobs` is a device array of `njobs` jobs that all share log_n, or NULL to
  * launch the single job `one` passed by value.  `scratch` (large n only)
