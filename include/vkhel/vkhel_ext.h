@@ -97,6 +97,38 @@ int vkhel_vector_polymul(const struct vkhel_vector *a,
 		const struct vkhel_vector *b, struct vkhel_vector *result,
 		struct vkhel_ntt_tables *ntt);
 
+/* ---- centred-lift epilogues ----
+ * Up to VKHEL_MAX_LIFT_STEPS of the reference's element-wise ops applied, in
+ * order, to the output of an inverse transform or polymul, inside the same
+ * kernel for 256 <= n <= 131072 (a separate element-wise launch otherwise).
+ * Results equal calling the reference functions one after another on the
+ * result vector (src/vector.c:342-386, 429-511):
+ *   VKHEL_LIFT_ELEMMOD    p0 = mod, p1 = q          vkhel_vector_elemmod
+ *   VKHEL_LIFT_ELEMGTSUB  p0 = bound, p1 = diff, p2 = mod   vkhel_vector_elemgtsub
+ *   VKHEL_LIFT_ELEMGTADD  p0 = bound, p1 = diff     vkhel_vector_elemgtadd
+ * ELEMMOD with p1 = 0 takes q from the transform's tables (in a batch, from
+ * each limb's tables): the BFV-style centred reduction of every limb. */
+enum vkhel_lift_op {
+	VKHEL_LIFT_ELEMMOD = 1,
+	VKHEL_LIFT_ELEMGTSUB = 2,
+	VKHEL_LIFT_ELEMGTADD = 3
+};
+#define VKHEL_MAX_LIFT_STEPS 4
+struct vkhel_lift_step {
+	uint32_t op;
+	uint64_t p0, p1, p2;
+};
+/* vkhel_vector_polymul, then the steps on the n result words. */
+int vkhel_vector_polymul_lift(const struct vkhel_vector *a,
+		const struct vkhel_vector *b, struct vkhel_vector *result,
+		struct vkhel_ntt_tables *ntt, const struct vkhel_lift_step *steps,
+		uint32_t nsteps);
+/* vkhel_vector_inverse_transform, then the steps on every result word (the
+ * reference's element-wise ops cover the whole result vector). */
+int vkhel_vector_inverse_transform_lift(const struct vkhel_vector *a,
+		struct vkhel_vector *result, struct vkhel_ntt_tables *ntt,
+		const struct vkhel_lift_step *steps, uint32_t nsteps);
+
 /* Same product as vkhel_vector_polymul without allocating any device memory
  * (no counterpart in the reference).  For callers that may not allocate at
  * the call site -- e.g. while a stream is being captured into a CUDA graph, or
@@ -134,6 +166,12 @@ int vkhel_batch_add_polymul(struct vkhel_batch *batch,
 int vkhel_batch_add_polymul_raw(struct vkhel_batch *batch,
 		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *b, uint64_t *c);
+/* vkhel_batch_add_polymul with a centred-lift epilogue on every limb. */
+int vkhel_batch_add_polymul_lift(struct vkhel_batch *batch,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *a, const struct vkhel_vector *b,
+		struct vkhel_vector *c, const struct vkhel_lift_step *steps,
+		uint32_t nsteps);
 int vkhel_batch_commit(struct vkhel_batch *batch, uint32_t flags);
 /* Enqueue one run on the context stream and return (asynchronous). */
 int vkhel_batch_launch(struct vkhel_batch *batch);

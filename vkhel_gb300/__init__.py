@@ -73,9 +73,12 @@ _SIGNATURES = [
     ("vkhel_vector_elemfma_canonical", None, [vp, vp, vp, u64, u64]),
     ("vkhel_vector_polymul", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_vector_polymul_noalloc", ctypes.c_int, [vp, vp, vp, vp]),
+    ("vkhel_vector_polymul_lift", ctypes.c_int, [vp, vp, vp, vp, vp, u32]),
+    ("vkhel_vector_inverse_transform_lift", ctypes.c_int, [vp, vp, vp, vp, u32]),
     ("vkhel_batch_create", vp, [vp]),
     ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_batch_add_polymul_lift", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp, vp, u32]),
     ("vkhel_batch_commit", ctypes.c_int, [vp, u32]),
     ("vkhel_batch_launch", ctypes.c_int, [vp]),
     ("vkhel_batch_run", ctypes.c_int, [vp]),
@@ -362,6 +365,40 @@ def polymul_noalloc(a, b, res, tables):
     _status(res.ctx.ptr, lib().vkhel_vector_polymul_noalloc(a.ptr, b.ptr, res.ptr, tables.ptr))
 
 
+# Centred-lift epilogue steps (struct vkhel_lift_step): the reference's
+# element-wise ops applied in order after the inverse transform.
+LIFT_ELEMMOD, LIFT_ELEMGTSUB, LIFT_ELEMGTADD = 1, 2, 3
+MAX_LIFT_STEPS = 4
+
+
+class LiftStep(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_uint32), ("p0", ctypes.c_uint64), ("p1", ctypes.c_uint64), ("p2", ctypes.c_uint64)]
+
+
+def lift_steps(steps):
+    """[("elemmod", mod, q), ("elemgtsub", bound, diff, mod), ("elemgtadd", bound, diff)] -> C array.
+
+    elemmod with q = 0 takes q from the transform's tables (each limb's, in a batch)."""
+    ops = {"elemmod": LIFT_ELEMMOD, "elemgtsub": LIFT_ELEMGTSUB, "elemgtadd": LIFT_ELEMGTADD}
+    arr = (LiftStep * max(1, len(steps)))()
+    for i, st in enumerate(steps):
+        op = ops.get(st[0], st[0])
+        params = [int(x) for x in st[1:]] + [0, 0, 0]
+        arr[i] = LiftStep(int(op), *params[:3])
+    return arr, len(steps)
+
+
+def polymul_lift(a, b, res, tables, steps):
+    arr, n = lift_steps(steps)
+    _status(res.ctx.ptr, lib().vkhel_vector_polymul_lift(a.ptr, b.ptr, res.ptr, tables.ptr, ctypes.addressof(arr), n))
+
+
+def inverse_transform_lift(a, res, tables, steps):
+    arr, n = lift_steps(steps)
+    _status(res.ctx.ptr, lib().vkhel_vector_inverse_transform_lift(a.ptr, res.ptr, tables.ptr,
+                                                                   ctypes.addressof(arr), n))
+
+
 def launch_count():
     return lib().vkhel_launch_count()
 
@@ -377,10 +414,14 @@ class Batch:
         self._keep = []
         ctx._children.add(self)
 
-    def add_polymul(self, tables, a, b, c):
+    def add_polymul(self, tables, a, b, c, lift=None):
         arr = (vp * len(tables))(*[t.ptr for t in tables])
         self._keep.append(tables)
-        if isinstance(a, Vector):
+        if lift:
+            steps, n = lift_steps(lift)
+            code = lib().vkhel_batch_add_polymul_lift(self.ptr, arr, len(tables), a.ptr, b.ptr, c.ptr,
+                                                      ctypes.addressof(steps), n)
+        elif isinstance(a, Vector):
             code = lib().vkhel_batch_add_polymul(self.ptr, arr, len(tables), a.ptr, b.ptr, c.ptr)
         else:  # raw device pointers
             code = lib().vkhel_batch_add_polymul_raw(self.ptr, arr, len(tables), int(a), int(b), int(c))

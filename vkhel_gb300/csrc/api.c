@@ -465,16 +465,21 @@ void vkhel_vector_forward_transform(const struct vkhel_vector *a, struct vkhel_v
 			"forward_transform");
 }
 
-void vkhel_vector_inverse_transform(const struct vkhel_vector *a, struct vkhel_vector *res,
-		struct vkhel_ntt_tables *t) {
+static int inverse_impl(const struct vkhel_vector *a, struct vkhel_vector *res, struct vkhel_ntt_tables *t,
+		const struct vkhel_lift_step *steps, uint32_t nsteps) {
 	const struct vkh_devtab *d = NULL;
-	if (check_transform("inverse_transform", a, res, t, &d))
-		return;
+	int st = check_transform("inverse_transform", a, res, t, &d);
+	if (st)
+		return st;
 	struct vkhel_ctx *ctx = res->ctx;
+	vkcu_lift lift;
+	if ((st = vkh_lift_compile(ctx, steps, nsteps, t->q, &lift)))
+		return st;
+	const vkcu_lift *lp = lift.count ? &lift : NULL;
 	int e = 0;
 	if (t->n > 1) {
 		const vkcu_ntt_job job = {a->dev, res->dev, d->dev_set};
-		e = vkcu_ntt_inverse(ctx->stream, NULL, 1, &job, t->log_n, ctx->sms);
+		e = vkcu_ntt_inverse_lift(ctx->stream, NULL, 1, &job, t->log_n, ctx->sms, lp);
 	}
 	/* src/vector.c:635-638 scales result->length words by n^-1: words past n
 	 * (and, for n == 1, the untouched result) are scaled here. */
@@ -482,11 +487,94 @@ void vkhel_vector_inverse_transform(const struct vkhel_vector *a, struct vkhel_v
 	if (!e && res->length > from)
 		e = vkcu_elemmulconst(ctx->stream, res->dev + from, res->dev + from, res->length - from, t->ninv, t->ninv_s,
 				t->q);
-	finish(ctx, e, "inverse_transform");
+	if (!e && res->length > from)
+		e = vkcu_lift_range(ctx->stream, res->dev + from, res->length - from, t->q, lp);
+	return finish(ctx, e, "inverse_transform");
 }
+
+void vkhel_vector_inverse_transform(const struct vkhel_vector *a, struct vkhel_vector *res,
+		struct vkhel_ntt_tables *t) {
+	inverse_impl(a, res, t, NULL, 0);
+}
+
+int vkhel_vector_inverse_transform_lift(const struct vkhel_vector *a, struct vkhel_vector *res,
+		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
+	return inverse_impl(a, res, t, steps, nsteps);
+}
+
+/* The reference's element-wise ops as epilogue steps, with the constants its
+ * host wrappers derive (src/vector.c:342-386, 429-511; the same derivations
+ * as vkhel_vector_elemmod / elemgtsub / elemgtadd above). */
+int vkh_lift_compile(struct vkhel_ctx *ctx, const struct vkhel_lift_step *steps, uint32_t nsteps, uint64_t q,
+		vkcu_lift *out) {
+	memset(out, 0, sizeof *out);
+	if (nsteps == 0)
+		return VKHEL_OK;
+	if (!steps || nsteps > VKCU_MAX_LIFT)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "lift: %u steps (1..%d)", nsteps, VKCU_MAX_LIFT);
+	for (uint32_t i = 0; i < nsteps; i++) {
+		const struct vkhel_lift_step *s = &steps[i];
+		vkcu_lift_step *d = &out->step[i];
+		switch (s->op) {
+		case VKHEL_LIFT_ELEMMOD: {
+			const uint64_t qq = s->p1 ? s->p1 : q;
+			const uint32_t tq = qq ? 0 : VKCU_LIFT_TABLE_Q;
+			if (s->p0 == 2) {
+				d->kind = VKCU_LIFT_MODTWO | tq;
+				d->bound = qq / 2;
+				break;
+			}
+			const int st = check_mod(ctx, "lift elemmod", s->p0);
+			if (st)
+				return st;
+			d->kind = VKCU_LIFT_GTSUB | tq;
+			d->mod = s->p0;
+			d->mu = vkh_barrett_mu(s->p0);
+			d->bits = (uint32_t) vkh_bitlen(s->p0);
+			d->bound = qq / 2;
+			d->d = vkh_ref_reduce64(qq, d->mod, d->mu);
+			break;
+		}
+		case VKHEL_LIFT_ELEMGTSUB: {
+			const int st = check_mod(ctx, "lift elemgtsub", s->p2);
+			if (st)
+				return st;
+			d->kind = VKCU_LIFT_GTSUB;
+			d->mod = s->p2;
+			d->mu = vkh_barrett_mu(s->p2);
+			d->bits = (uint32_t) vkh_bitlen(s->p2);
+			d->bound = s->p0;
+			d->d = vkh_ref_reduce64(s->p1, d->mod, d->mu);
+			break;
+		}
+		case VKHEL_LIFT_ELEMGTADD:
+			d->kind = VKCU_LIFT_GTADD;
+			d->bound = s->p0;
+			d->d = s->p1;
+			break;
+		default:
+			return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "lift: step %u has unknown op %u", i, s->op);
+		}
+	}
+	out->count = nsteps;
+	return VKHEL_OK;
+}
+
+static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
+		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps);
 
 int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t) {
+	return polymul_impl(a, b, res, t, NULL, 0);
+}
+
+int vkhel_vector_polymul_lift(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
+		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
+	return polymul_impl(a, b, res, t, steps, nsteps);
+}
+
+static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
+		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
 	const struct vkh_devtab *d = NULL;
 	int st = check_transform("polymul", a, res, t, &d);
 	if (st)
@@ -494,10 +582,17 @@ int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector
 	if (!b || b->ctx != res->ctx || b->length < t->n)
 		return vkh_fail(res->ctx, VKHEL_ERR_INVALID_ARGUMENT, "polymul: bad operand b");
 	struct vkhel_ctx *ctx = res->ctx;
+	vkcu_lift lift;
+	if ((st = vkh_lift_compile(ctx, steps, nsteps, t->q, &lift)))
+		return st;
+	const vkcu_lift *lp = lift.count ? &lift : NULL;
 	const uint64_t bytes = t->n * sizeof(uint64_t);
 	if (t->n == 1) {
 		/* forward is a no-op at n = 1 and inverse scales by 1 */
-		return finish(ctx, vkcu_elemmul(ctx->stream, res->dev, a->dev, b->dev, 1, t->q, t->mu, t->qbits), "polymul");
+		int e = vkcu_elemmul(ctx->stream, res->dev, a->dev, b->dev, 1, t->q, t->mu, t->qbits);
+		if (!e)
+			e = vkcu_lift_range(ctx->stream, res->dev, 1, t->q, lp);
+		return finish(ctx, e, "polymul");
 	}
 	uint64_t *scratch = res->dev;
 	void *tmp = NULL;
@@ -513,7 +608,7 @@ int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector
 	int e;
 	if (fused) {
 		const vkcu_poly_job job = {a->dev, b->dev, res->dev, scratch, d->dev_set};
-		e = vkcu_polymul(ctx->stream, NULL, 1, &job, t->log_n, ctx->sms);
+		e = vkcu_polymul_lift(ctx->stream, NULL, 1, &job, t->log_n, ctx->sms, lp);
 	} else {
 		const vkcu_ntt_job jb = {b->dev, scratch, d->dev_set};
 		const vkcu_ntt_job ja = {a->dev, res->dev, d->dev_set};
@@ -524,7 +619,7 @@ int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector
 		if (!e)
 			e = vkcu_elemmul(ctx->stream, res->dev, res->dev, scratch, t->n, t->q, t->mu, t->qbits);
 		if (!e)
-			e = vkcu_ntt_inverse(ctx->stream, NULL, 1, &jc, t->log_n, ctx->sms);
+			e = vkcu_ntt_inverse_lift(ctx->stream, NULL, 1, &jc, t->log_n, ctx->sms, lp);
 	}
 	st = finish(ctx, e, "polymul");
 	if (tmp)

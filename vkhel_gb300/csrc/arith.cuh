@@ -90,4 +90,25 @@ __device__ __forceinline__ u64 barrett_mul_lazy(u64 x, u64 y, u64 q, u64 q2, u64
   return csub(lo - qh * q, q2);
 }
 
+// The reference's centred-lift element-wise ops on one word, as their
+// shaders compute them (64-bit wrap included):
+//   elemgtsub    src/kernels/shaders/elemgtsub.comp:49-67 (d = diff reduced mod `mod`)
+//   elemgtadd    src/kernels/shaders/elemgtadd.comp:20-30
+//   elemmodbytwo src/kernels/shaders/elemmodbytwo.comp:19-27 (sb = q / 2)
+__device__ __forceinline__ u64 ref_gtsub(u64 a, u64 bound, u64 d, u64 mod, u64 mu, u32 bits) {
+  const u64 r = ref_reduce64(a, mod, mu, bits);
+  if (a > bound) {
+    const u64 z = r + mod - d;
+    return z >= mod ? z - mod : z;
+  }
+  return r;
+}
+
+__device__ __forceinline__ u64 ref_gtadd(u64 a, u64 bound, u64 diff) { return a > bound ? a + diff : a; }
+
+__device__ __forceinline__ u64 ref_modtwo(u64 a, u64 sb) {
+  const u64 bit = a & 1;
+  return a > sb ? 1 - bit : bit;
+}
+
 }  // namespace vk

@@ -23,6 +23,8 @@
 struct job_rec {
 	uint32_t log_n;
 	uint32_t needs_scratch;
+	uint32_t lift;         /* index into the batch's lift table, 0 = none */
+	uint32_t order;        /* insertion order, keeps the sort stable */
 	vkcu_poly_job job;
 };
 
@@ -31,6 +33,8 @@ struct vkhel_batch {
 	struct job_rec *recs;
 	uint32_t njobs, cap;
 	int committed;
+	vkcu_lift *lifts;      /* [0] unused (no epilogue) */
+	uint32_t nlifts;
 	uint32_t flags;
 	struct vkh_job_class classes[MAX_CLASSES];
 	uint32_t nclasses;
@@ -63,8 +67,31 @@ struct vkhel_batch *vkhel_batch_create(struct vkhel_ctx *ctx) {
 	return b;
 }
 
+/* Index of `l` in the batch's lift table (added when new); 0 for none. */
+static int lift_index(struct vkhel_batch *b, const vkcu_lift *l, uint32_t *idx) {
+	*idx = 0;
+	if (!l || l->count == 0)
+		return VKHEL_OK;
+	for (uint32_t i = 1; i < b->nlifts; i++) {
+		if (!memcmp(&b->lifts[i], l, sizeof *l)) {
+			*idx = i;
+			return VKHEL_OK;
+		}
+	}
+	const uint32_t n = b->nlifts ? b->nlifts : 1;
+	vkcu_lift *t = realloc(b->lifts, sizeof(*t) * (n + 1));
+	if (!t)
+		return vkh_fail(b->ctx, VKHEL_ERR_OUT_OF_MEMORY, "batch_add: host allocation failed");
+	memset(&t[0], 0, sizeof t[0]);
+	t[n] = *l;
+	b->lifts = t;
+	b->nlifts = n + 1;
+	*idx = n;
+	return VKHEL_OK;
+}
+
 static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
-		const uint64_t *a, const uint64_t *bb, uint64_t *c) {
+		const uint64_t *a, const uint64_t *bb, uint64_t *c, const vkcu_lift *lift) {
 	struct vkhel_ctx *ctx = b->ctx;
 	if (b->committed)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch: already committed");
@@ -80,6 +107,10 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_log_n())
 			return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_add: limb %u (n, q) unsupported", k);
 	}
+	uint32_t lift_id = 0;
+	const int lst = lift_index(b, lift, &lift_id);
+	if (lst)
+		return lst;
 	if (b->njobs + limbs > b->cap) {
 		uint32_t cap = b->cap ? b->cap : 64;
 		while (cap < b->njobs + limbs)
@@ -104,6 +135,8 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		const int overlap = ak < ck + n && ck < ak + n;
 		r->log_n = log_n;
 		r->needs_scratch = !fused || overlap;
+		r->lift = lift_id;
+		r->order = b->njobs - 1;
 		r->job.a = ak;
 		r->job.b = bk;
 		r->job.c = ck;
@@ -124,32 +157,58 @@ int vkhel_batch_add_polymul(struct vkhel_batch *b, struct vkhel_ntt_tables *cons
 	const uint64_t need = (uint64_t) limbs * tables[0]->n;
 	if (a->length < need || bb->length < need || c->length < need)
 		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors shorter than limbs * n");
-	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev);
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, NULL);
+}
+
+int vkhel_batch_add_polymul_lift(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *a, const struct vkhel_vector *bb, struct vkhel_vector *c,
+		const struct vkhel_lift_step *steps, uint32_t nsteps) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
+	if (!a || !bb || !c || !tables || !tables[0])
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL argument");
+	if (a->ctx != b->ctx || bb->ctx != b->ctx || c->ctx != b->ctx)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors of another context");
+	const uint64_t need = (uint64_t) limbs * tables[0]->n;
+	if (a->length < need || bb->length < need || c->length < need)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors shorter than limbs * n");
+	/* ELEMMOD with q = 0 resolves each limb's modulus on the device */
+	vkcu_lift lift;
+	const int st = vkh_lift_compile(b->ctx, steps, nsteps, 0, &lift);
+	if (st)
+		return st;
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, &lift);
 }
 
 int vkhel_batch_add_polymul_raw(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *bb, uint64_t *c) {
 	if (!b)
 		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
-	return add_jobs(b, tables, limbs, a, bb, c);
+	return add_jobs(b, tables, limbs, a, bb, c, NULL);
 }
 
 static int cmp_rec(const void *x, const void *y) {
 	const struct job_rec *a = x, *b = y;
-	return (a->log_n > b->log_n) - (a->log_n < b->log_n);
+	if (a->log_n != b->log_n)
+		return (a->log_n > b->log_n) - (a->log_n < b->log_n);
+	if (a->lift != b->lift)
+		return (a->lift > b->lift) - (a->lift < b->lift);
+	return (a->order > b->order) - (a->order < b->order);
 }
 
 /* Launch the kernels of `nclasses` degree classes on `stream`: one fused
- * polymul launch per class with 2^8 <= n <= 2^14, otherwise forward(b ->
+ * polymul launch per class with 2^8 <= n <= 2^17, otherwise forward(b ->
  * scratch), forward(a -> c), pointwise, inverse(c) over the class's slice of
- * the ntt-job array (laid out at 3 * first: b jobs, a jobs, c jobs). */
+ * the ntt-job array (laid out at 3 * first: b jobs, a jobs, c jobs).  A
+ * class's epilogue rides on its last launch. */
 int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt,
-		const struct vkh_job_class *classes, uint32_t nclasses) {
+		const struct vkh_job_class *classes, uint32_t nclasses, const vkcu_lift *lifts) {
 	for (uint32_t k = 0; k < nclasses; k++) {
 		const struct vkh_job_class *cl = &classes[k];
+		const vkcu_lift *lift = lifts && cl->lift ? &lifts[cl->lift] : NULL;
 		int e;
 		if (cl->fused) {
-			e = vkcu_polymul(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, sms);
+			e = vkcu_polymul_lift(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, sms, lift);
 		} else {
 			const vkcu_ntt_job *nj = dev_ntt + 3 * (size_t) cl->first;
 			e = vkcu_ntt_forward(stream, nj, (int) cl->count, NULL, cl->log_n, sms);
@@ -158,7 +217,8 @@ int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, cons
 			if (!e)
 				e = vkcu_pointwise(stream, dev_poly + cl->first, (int) cl->count, cl->log_n, sms);
 			if (!e)
-				e = vkcu_ntt_inverse(stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n, sms);
+				e = vkcu_ntt_inverse_lift(stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n, sms,
+						lift);
 		}
 		if (e)
 			return e;
@@ -189,14 +249,14 @@ void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struc
  * also how a CUDA graph capture picks up the parallel branches). */
 int vkh_issue_classes_forked(void *stream, void *const *aux, void *fork, void *const *join, int sms,
 		const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt, const struct vkh_job_class *classes,
-		uint32_t nclasses) {
+		uint32_t nclasses, const vkcu_lift *lifts) {
 	if (nclasses < 2)
-		return vkh_issue_classes(stream, sms, dev_poly, dev_ntt, classes, nclasses);
+		return vkh_issue_classes(stream, sms, dev_poly, dev_ntt, classes, nclasses, lifts);
 	int e = vkcu_event_record(fork, stream);
 	for (uint32_t k = 1; !e && k < nclasses; k++)
 		e = vkcu_stream_wait(aux[k - 1], fork);
 	for (uint32_t k = 0; !e && k < nclasses; k++)
-		e = vkh_issue_classes(k ? aux[k - 1] : stream, sms, dev_poly, dev_ntt, &classes[k], 1);
+		e = vkh_issue_classes(k ? aux[k - 1] : stream, sms, dev_poly, dev_ntt, &classes[k], 1, lifts);
 	for (uint32_t k = 1; !e && k < nclasses; k++) {
 		e = vkcu_event_record(join[k - 1], aux[k - 1]);
 		if (!e)
@@ -208,8 +268,9 @@ int vkh_issue_classes_forked(void *stream, void *const *aux, void *fork, void *c
 static int issue(struct vkhel_batch *b) {
 	if (b->naux)
 		return vkh_issue_classes_forked(b->ctx->stream, b->aux, b->fork, b->join, b->ctx->sms, b->dev_poly,
-				b->dev_ntt, b->classes, b->nclasses);
-	return vkh_issue_classes(b->ctx->stream, b->ctx->sms, b->dev_poly, b->dev_ntt, b->classes, b->nclasses);
+				b->dev_ntt, b->classes, b->nclasses, b->lifts);
+	return vkh_issue_classes(b->ctx->stream, b->ctx->sms, b->dev_poly, b->dev_ntt, b->classes, b->nclasses,
+			b->lifts);
 }
 
 int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
@@ -227,11 +288,13 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	b->nclasses = 0;
 	for (uint32_t i = 0; i < b->njobs; i++) {
 		struct job_rec *r = &b->recs[i];
-		if (b->nclasses == 0 || b->classes[b->nclasses - 1].log_n != r->log_n) {
+		if (b->nclasses == 0 || b->classes[b->nclasses - 1].log_n != r->log_n ||
+				b->classes[b->nclasses - 1].lift != r->lift) {
 			if (b->nclasses == MAX_CLASSES)
 				return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_commit: too many degree classes");
 			struct vkh_job_class *cl = &b->classes[b->nclasses++];
 			cl->log_n = r->log_n;
+			cl->lift = r->lift;
 			cl->first = i;
 			cl->count = 0;
 			cl->fused = r->log_n >= 8 && r->log_n <= vkcu_max_fused_log_n();
@@ -358,5 +421,6 @@ void vkhel_batch_destroy(struct vkhel_batch *b) {
 	vkh_dev_free(ctx, b->dev, b->dev_bytes);
 	vkh_dev_free(ctx, b->scratch, b->scratch_bytes);
 	free(b->recs);
+	free(b->lifts);
 	free(b);
 }

@@ -65,27 +65,17 @@ struct OpFmaCanon {
 struct OpGtSub {
   u64 bound, d, mod, mu;
   u32 bits;
-  __device__ __forceinline__ u64 operator()(u64 a, u64) const {
-    const u64 r = ref_reduce64(a, mod, mu, bits);
-    if (a > bound) {
-      const u64 z = r + mod - d;
-      return z >= mod ? z - mod : z;
-    }
-    return r;
-  }
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const { return ref_gtsub(a, bound, d, mod, mu, bits); }
 };
 
 struct OpGtAdd {
   u64 bound, diff;
-  __device__ __forceinline__ u64 operator()(u64 a, u64) const { return a > bound ? a + diff : a; }
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const { return ref_gtadd(a, bound, diff); }
 };
 
 struct OpModTwo {
   u64 sb;
-  __device__ __forceinline__ u64 operator()(u64 a, u64) const {
-    const u64 bit = a & 1;
-    return a > sb ? 1 - bit : bit;
-  }
+  __device__ __forceinline__ u64 operator()(u64 a, u64) const { return ref_modtwo(a, sb); }
 };
 
 __device__ __forceinline__ ulonglong2 ld2(const u64* p) {

@@ -86,17 +86,23 @@ void vkh_dev_free(struct vkhel_ctx *ctx, void *ptr, uint64_t bytes);
 int vkh_devtab_get(struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t,
 		const struct vkh_devtab **out);
 void vkh_devtab_release_all(struct vkhel_ctx *ctx);
+/* api.c -- centred-lift steps to the device form; q = 0 leaves ELEMMOD's
+ * modulus to each job's tables */
+int vkh_lift_compile(struct vkhel_ctx *ctx, const struct vkhel_lift_step *steps, uint32_t nsteps, uint64_t q,
+		vkcu_lift *out);
 /* batch.c -- degree classes of a sorted job list, shared with the server */
 struct vkh_job_class {
 	uint32_t log_n;
 	uint32_t first, count;
 	int fused;
+	uint32_t lift;         /* index into the lift table, 0 = none */
 };
+/* lifts: table indexed by vkh_job_class.lift (NULL when no class has one) */
 int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt,
-		const struct vkh_job_class *classes, uint32_t nclasses);
+		const struct vkh_job_class *classes, uint32_t nclasses, const vkcu_lift *lifts);
 int vkh_issue_classes_forked(void *stream, void *const *aux, void *fork, void *const *join, int sms,
 		const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt, const struct vkh_job_class *classes,
-		uint32_t nclasses);
+		uint32_t nclasses, const vkcu_lift *lifts);
 void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struct vkh_job_class *classes,
 		uint32_t nclasses);
 /* tuning.c -- variant of kernel family (VKHEL_TUNE_*) for degree 2^log_n */

@@ -99,6 +99,22 @@ int vkcu_elemmodbytwo(void *stream, uint64_t *res, const uint64_t *a,
 int vkcu_twiddles(void *stream, uint64_t *fwd, uint64_t *inv, const uint64_t *phi,
 		const uint64_t *plo, uint32_t log_n, uint32_t lb, uint64_t q, uint64_t mu, uint32_t qbits);
 
+/* Epilogue of an inverse transform or polymul: the reference's elemmod /
+ * elemgtsub / elemgtadd applied in order to every output word.  With
+ * VKCU_LIFT_TABLE_Q the step takes bound = q / 2 (and, for GTSUB, d = q
+ * reduced mod `mod`) from the job's own modulus. */
+enum { VKCU_LIFT_MODTWO = 1, VKCU_LIFT_GTSUB = 2, VKCU_LIFT_GTADD = 3 };
+#define VKCU_LIFT_TABLE_Q 0x100u
+#define VKCU_MAX_LIFT 4
+typedef struct vkcu_lift_step {
+	uint32_t kind, bits;         /* kind | VKCU_LIFT_TABLE_Q; bits = bitlen(mod) */
+	uint64_t bound, d, mod, mu;  /* d: reduced diff (GTSUB) or diff (GTADD) */
+} vkcu_lift_step;
+typedef struct vkcu_lift {
+	uint32_t count, pad;
+	vkcu_lift_step step[VKCU_MAX_LIFT];
+} vkcu_lift;
+
 /* ---- transforms (ntt.cu) ----
  * `jobs` is a device array of `njobs` jobs that all share log_n, or NULL to
  * launch the single job `one` passed by value.  `scratch` (large n only)
@@ -109,6 +125,17 @@ int vkcu_ntt_inverse(void *stream, const vkcu_ntt_job *jobs, int njobs,
 		const vkcu_ntt_job *one, uint32_t log_n, int sms);
 int vkcu_polymul(void *stream, const vkcu_poly_job *jobs, int njobs,
 		const vkcu_poly_job *one, uint32_t log_n, int sms);
+/* The same with an epilogue (`lift` NULL or count 0: none); fused into the
+ * last pass for 2^8 <= n <= 2^17, a separate element-wise launch otherwise. */
+int vkcu_ntt_inverse_lift(void *stream, const vkcu_ntt_job *jobs, int njobs,
+		const vkcu_ntt_job *one, uint32_t log_n, int sms, const vkcu_lift *lift);
+int vkcu_polymul_lift(void *stream, const vkcu_poly_job *jobs, int njobs,
+		const vkcu_poly_job *one, uint32_t log_n, int sms, const vkcu_lift *lift);
+/* The epilogue alone, in place on `len` words at p (modulus q for TABLE_Q
+ * steps), or on the n output words of every job. */
+int vkcu_lift_range(void *stream, uint64_t *p, uint64_t len, uint64_t q, const vkcu_lift *lift);
+int vkcu_lift_jobs(void *stream, const vkcu_ntt_job *jobs, int njobs, const vkcu_ntt_job *one,
+		uint32_t log_n, int sms, const vkcu_lift *lift);
 /* c = c * scratch mod q (lazy inputs from the forward transforms, canonical
  * output) for every job: the pointwise step of a polymul that is not fused. */
 int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,

@@ -205,28 +205,106 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
   return fwd_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(1, kMaxCta));
 }
 
-extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
-                                uint32_t log_n, int sms) {
+static bool has_lift(const vkcu_lift* lift) { return lift && lift->count > 0; }
+
+extern "C" int vkcu_ntt_inverse_lift(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
+                                     uint32_t log_n, int sms, const vkcu_lift* lift) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
   if (log_n < 1 || log_n > (uint32_t)kMaxLogN || njobs < 1) return (int)cudaErrorInvalidValue;
+  if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
   const bool aligned = jobs_aligned(jobs, one);
-  if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, true, jobs, njobs, o, (int)log_n, sms);
-  if (!aligned) return (int)cudaErrorMisalignedAddress;
-  if (log_n <= (uint32_t)kMaxCta) return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(2, (int)log_n));
-  if (log_n <= (uint32_t)kMaxCluster) return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
-  const int kk = (int)log_n - kMaxCta;
-  if (int e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(2, kMaxCta))) return e;
-  return global_pass<true>(st, jobs, njobs, o, (int)log_n, kk, sms);
+  const bool lifted = has_lift(lift);
+  int e;
+  if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) {
+    e = simple(st, true, jobs, njobs, o, (int)log_n, sms);
+  } else if (!aligned) {
+    return (int)cudaErrorMisalignedAddress;
+  } else if (log_n <= (uint32_t)kMaxCta) {
+    if (lifted) return inv_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
+    return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(2, (int)log_n));
+  } else if (log_n <= (uint32_t)kMaxCluster) {
+    return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, lifted ? lift : nullptr);
+  } else {
+    const int kk = (int)log_n - kMaxCta;
+    e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(2, kMaxCta));
+    if (!e) e = global_pass<true>(st, jobs, njobs, o, (int)log_n, kk, sms);
+  }
+  // the multi-launch paths take the epilogue as one more element-wise launch
+  if (!e && lifted) e = vkcu_lift_jobs(stream, jobs, njobs, one, log_n, sms, lift);
+  return e;
+}
+
+extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
+                                uint32_t log_n, int sms) {
+  return vkcu_ntt_inverse_lift(stream, jobs, njobs, one, log_n, sms, nullptr);
+}
+
+extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,
+                                 uint32_t log_n, int sms, const vkcu_lift* lift) {
+  cudaStream_t st = (cudaStream_t)stream;
+  const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
+  if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
+  if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
+  if (log_n <= (uint32_t)kMaxCta) {
+    if (has_lift(lift)) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
+    return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
+  }
+  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, has_lift(lift) ? lift : nullptr);
 }
 
 extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,
                             uint32_t log_n, int sms) {
-  cudaStream_t st = (cudaStream_t)stream;
-  const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
-  if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
-  if (log_n <= (uint32_t)kMaxCta) return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
-  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
+  return vkcu_polymul_lift(stream, jobs, njobs, one, log_n, sms, nullptr);
+}
+
+// The epilogue as its own element-wise pass: over `len` words at p, or over
+// the n output words of each job (q from the job's twiddle set).
+__global__ void k_lift_range(u64* __restrict__ p, u64 len, u64 q, const __grid_constant__ vkcu_lift lift) {
+  const LiftRun lr(&lift, q);
+  for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < len; i += (u64)gridDim.x * blockDim.x)
+    p[i] = lr(p[i]);
+}
+
+__global__ void k_lift_jobs(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int log_n,
+                            const __grid_constant__ vkcu_lift lift) {
+  const long n = 1L << log_n;
+  const long per = (n + gridDim.y - 1) / gridDim.y;  // words of a job per block row
+  for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
+    const vkcu_ntt_job job = fetch_job(jobs, one, w);
+    const LiftRun lr(&lift, load_tw(job.tw).q);
+    u64* out = reinterpret_cast<u64*>(job.out);
+    const long lo = (long)blockIdx.y * per, hi = lo + per < n ? lo + per : n;
+    for (long i = lo + threadIdx.x; i < hi; i += blockDim.x) out[i] = lr(out[i]);
+  }
+}
+
+extern "C" int vkcu_lift_range(void* stream, uint64_t* p, uint64_t len, uint64_t q, const vkcu_lift* lift) {
+  if (!has_lift(lift) || len == 0) return 0;
+  if (lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
+  uint64_t blocks = (len + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_lift_range<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<u64*>(p), len, q, *lift);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
+                              uint32_t log_n, int sms, const vkcu_lift* lift) {
+  if (!has_lift(lift)) return 0;
+  if (njobs < 1 || log_n > (uint32_t)kMaxLogN || lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
+  const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
+  const long n = 1L << log_n;
+  const int threads = n < 256 ? (int)((n + 31) / 32 * 32) : 256;
+  const long want = (long)(sms > 0 ? sms : 1) * 8;
+  const int gx = njobs < want ? njobs : (int)want;
+  long gy = (want + gx - 1) / gx;  // split each job when there are few
+  const long max_gy = (n + threads - 1) / threads;
+  if (gy > max_gy) gy = max_gy;
+  k_lift_jobs<<<dim3((unsigned)gx, (unsigned)gy), threads, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n,
+                                                                                      *lift);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
 }
 
 // Pointwise step of a composed polymul: c = c * scratch mod q over njobs

@@ -69,9 +69,9 @@ __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, con
 
 // Inverse column pass: gather, global stages LOGC-1 .. 0 with n^-1 folded in,
 // canonical words to global memory.
-template <int LOGC>
+template <int LOGC, class Epi>
 __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
-                                        const Tw& t) {
+                                        const Tw& t, const Epi& epi) {
   using K = Cols<LOGC>;
   u64 v[K::PER * K::C];
 #pragma unroll
@@ -87,7 +87,16 @@ __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg
 #pragma unroll
   for (int k = 0; k < K::PER; k++)
 #pragma unroll
-    for (int j = 0; j < K::C; j++) out[K::col(rank, k) + (size_t)j * K::SUB] = v[k * K::C + j];
+    for (int j = 0; j < K::C; j++) out[K::col(rank, k) + (size_t)j * K::SUB] = epi(v[k * K::C + j]);
+}
+
+template <int LOGC, bool LIFT>
+__device__ __forceinline__ void col_inv_out(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
+                                            const Tw& t, const vkcu_lift* lift) {
+  if constexpr (LIFT)
+    col_inv<LOGC>(out, sm, cl, rank, t, LiftRun(lift, t.q));
+  else
+    col_inv<LOGC>(out, sm, cl, rank, t, NoLift{});
 }
 
 template <int LOGC>
@@ -118,9 +127,10 @@ __global__ void __launch_bounds__(512, 1)
   cl.sync();
 }
 
-template <int LOGC>
+template <int LOGC, bool LIFT>
 __global__ void __launch_bounds__(512, 1)
-    k_ntt_inv_cluster(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one) {
+    k_ntt_inv_cluster(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
+                      const __grid_constant__ vkcu_lift lift) {
   using S = SubShape;
   using K = Cols<LOGC>;
   extern __shared__ u64 sm[];
@@ -147,14 +157,15 @@ __global__ void __launch_bounds__(512, 1)
     inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
     inv_last_smem<S>(sm, t, tw_mult);
     cl.sync();
-    col_inv<LOGC>(reinterpret_cast<u64*>(job.out), sm, cl, rank, t);
+    col_inv_out<LOGC, LIFT>(reinterpret_cast<u64*>(job.out), sm, cl, rank, t, &lift);
   }
   cl.sync();
 }
 
-template <int LOGC>
+template <int LOGC, bool LIFT>
 __global__ void __launch_bounds__(512, 1)
-    k_polymul_cluster(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one) {
+    k_polymul_cluster(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one,
+                      const __grid_constant__ vkcu_lift lift) {
   using S = SubShape;
   using K = Cols<LOGC>;
   extern __shared__ u64 sm[];
@@ -197,7 +208,7 @@ __global__ void __launch_bounds__(512, 1)
     inv_passes<S>(sm, t, tw_mult, S::HEAD);
     inv_last_smem<S>(sm, t, tw_mult);
     cl.sync();
-    col_inv<LOGC>(reinterpret_cast<u64*>(job.c), sm, cl, rank, t);
+    col_inv_out<LOGC, LIFT>(reinterpret_cast<u64*>(job.c), sm, cl, rank, t, &lift);
   }
   cl.sync();
 }
@@ -241,20 +252,30 @@ int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu
   }
 }
 
-int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc) {
-  switch (logc) {
-    case 1: return launch_cluster<1, k_ntt_inv_cluster<1>>(st, njobs, jobs, njobs, one);
-    case 2: return launch_cluster<2, k_ntt_inv_cluster<2>>(st, njobs, jobs, njobs, one);
-    case 3: return launch_cluster<3, k_ntt_inv_cluster<3>>(st, njobs, jobs, njobs, one);
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,
+                const vkcu_lift* lift) {
+  const vkcu_lift l = lift ? *lift : vkcu_lift{};
+  switch (logc * 2 + (lift ? 1 : 0)) {
+    case 2: return launch_cluster<1, k_ntt_inv_cluster<1, false>>(st, njobs, jobs, njobs, one, l);
+    case 3: return launch_cluster<1, k_ntt_inv_cluster<1, true>>(st, njobs, jobs, njobs, one, l);
+    case 4: return launch_cluster<2, k_ntt_inv_cluster<2, false>>(st, njobs, jobs, njobs, one, l);
+    case 5: return launch_cluster<2, k_ntt_inv_cluster<2, true>>(st, njobs, jobs, njobs, one, l);
+    case 6: return launch_cluster<3, k_ntt_inv_cluster<3, false>>(st, njobs, jobs, njobs, one, l);
+    case 7: return launch_cluster<3, k_ntt_inv_cluster<3, true>>(st, njobs, jobs, njobs, one, l);
     default: return (int)cudaErrorInvalidValue;
   }
 }
 
-int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc) {
-  switch (logc) {
-    case 1: return launch_cluster<1, k_polymul_cluster<1>>(st, njobs, jobs, njobs, one);
-    case 2: return launch_cluster<2, k_polymul_cluster<2>>(st, njobs, jobs, njobs, one);
-    case 3: return launch_cluster<3, k_polymul_cluster<3>>(st, njobs, jobs, njobs, one);
+int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
+                 const vkcu_lift* lift) {
+  const vkcu_lift l = lift ? *lift : vkcu_lift{};
+  switch (logc * 2 + (lift ? 1 : 0)) {
+    case 2: return launch_cluster<1, k_polymul_cluster<1, false>>(st, njobs, jobs, njobs, one, l);
+    case 3: return launch_cluster<1, k_polymul_cluster<1, true>>(st, njobs, jobs, njobs, one, l);
+    case 4: return launch_cluster<2, k_polymul_cluster<2, false>>(st, njobs, jobs, njobs, one, l);
+    case 5: return launch_cluster<2, k_polymul_cluster<2, true>>(st, njobs, jobs, njobs, one, l);
+    case 6: return launch_cluster<3, k_polymul_cluster<3, false>>(st, njobs, jobs, njobs, one, l);
+    case 7: return launch_cluster<3, k_polymul_cluster<3, true>>(st, njobs, jobs, njobs, one, l);
     default: return (int)cudaErrorInvalidValue;
   }
 }

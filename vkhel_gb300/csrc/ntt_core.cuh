@@ -364,8 +364,46 @@ __device__ __forceinline__ void inv_last_smem(u64* sm, const Tw& t, u32 tw_mult)
 // Last inverse pass (stages FIRSTK-1 .. 0) from shared memory to `out`,
 // coalesced.  fold: whole transform, n^-1 folded into stage 0, canonical
 // output; otherwise lazy [0, 2q).
-template <class S>
-__device__ __forceinline__ void inv_last(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, bool fold) {
+// Epilogue of the inverse transforms: the reference's centred-lift ops in
+// order on each canonical output word (src/vector.c:342-386, 429-511), with
+// the job's modulus resolved once per job for VKCU_LIFT_TABLE_Q steps.
+struct LiftRun {
+  const vkcu_lift* L;
+  u64 bound[VKCU_MAX_LIFT], d[VKCU_MAX_LIFT];
+  __device__ __forceinline__ LiftRun(const vkcu_lift* l, u64 q) : L(l) {
+#pragma unroll
+    for (int s = 0; s < VKCU_MAX_LIFT; s++) {
+      const vkcu_lift_step& st = L->step[s];
+      const bool tq = (st.kind & VKCU_LIFT_TABLE_Q) != 0;
+      bound[s] = tq ? q >> 1 : st.bound;
+      d[s] = tq && s < (int)L->count && (st.kind & 0xff) == VKCU_LIFT_GTSUB ? ref_reduce64(q, st.mod, st.mu, st.bits)
+                                                                              : st.d;
+    }
+  }
+  __device__ __forceinline__ u64 operator()(u64 x) const {
+#pragma unroll
+    for (int s = 0; s < VKCU_MAX_LIFT; s++) {
+      if (s >= (int)L->count) break;
+      const vkcu_lift_step& st = L->step[s];
+      const u32 kind = st.kind & 0xff;
+      if (kind == VKCU_LIFT_MODTWO)
+        x = ref_modtwo(x, bound[s]);
+      else if (kind == VKCU_LIFT_GTSUB)
+        x = ref_gtsub(x, bound[s], d[s], st.mod, st.mu, st.bits);
+      else
+        x = ref_gtadd(x, bound[s], d[s]);
+    }
+    return x;
+  }
+};
+
+struct NoLift {
+  __device__ __forceinline__ u64 operator()(u64 x) const { return x; }
+};
+
+template <class S, class Epi>
+__device__ __forceinline__ void inv_last_epi(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, bool fold,
+                                             const Epi& epi) {
   constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
 #pragma unroll 1
   for (int i = 0; i < G; i++) {
@@ -378,8 +416,19 @@ __device__ __forceinline__ void inv_last(u64* sm, const Tw& t, u32 tw_mult, u64*
     else
       gs_group<KK, 0, false, false>(v, t.inv, tw_mult, t);
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) out[g + j * TMIN] = v[j];
+    for (int j = 0; j < (1 << KK); j++) out[g + j * TMIN] = epi(v[j]);
   }
+}
+
+// Last inverse pass to global memory; LIFT applies the epilogue (only where
+// fold, i.e. this pass ends the transform).
+template <class S, bool LIFT = false>
+__device__ __forceinline__ void inv_last(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, bool fold,
+                                         const vkcu_lift* lift = nullptr) {
+  if constexpr (LIFT)
+    inv_last_epi<S>(sm, t, tw_mult, out, fold, LiftRun(lift, t.q));
+  else
+    inv_last_epi<S>(sm, t, tw_mult, out, fold, NoLift{});
 }
 
 // Register groups of 16 consecutive words <-> global memory (32-byte vectors).
@@ -437,9 +486,11 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
   }
 }
 
-template <int LOGN, int E, int U>
+// LIFT: the epilogue `lift` follows the last stage (sub_log == 0 only).
+template <int LOGN, int E, int U, bool LIFT = false>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
-    k_ntt_inv(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log) {
+    k_ntt_inv(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log,
+              const __grid_constant__ vkcu_lift lift) {
   using S = Shape<LOGN, E, U>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
@@ -463,7 +514,7 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     }
     __syncthreads();
     inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
-    inv_last<S>(sm, t, tw_mult, out, sub_log == 0);
+    inv_last<S, LIFT>(sm, t, tw_mult, out, sub_log == 0, &lift);
     __syncthreads();
   }
 }
@@ -473,9 +524,10 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
 // last pass multiplies by NTT(b) (read back at the words this thread wrote)
 // into shared memory; the inverse transform then writes c.  a is prefetched
 // into L2 while b is transformed, the next job's b while a is.
-template <int LOGN, int E, int U>
+template <int LOGN, int E, int U, bool LIFT = false>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
-    k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one) {
+    k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one,
+              const __grid_constant__ vkcu_lift lift) {
   using S = Shape<LOGN, E, U>;
   extern __shared__ u64 sm[];
   constexpr unsigned kChunk = (unsigned)(S::N * 8 / 4);
@@ -507,7 +559,7 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
       });
     }
     inv_passes<S>(sm, t, 1u, S::HEAD);
-    inv_last<S>(sm, t, 1u, reinterpret_cast<u64*>(job.c), true);
+    inv_last<S, LIFT>(sm, t, 1u, reinterpret_cast<u64*>(job.c), true, &lift);
     __syncthreads();
   }
 }
@@ -523,10 +575,17 @@ int inv_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt
             int sms, int variant);
 int poly_cta(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
              int variant);
+// With an epilogue: default shape of each degree, one CTA per transform.
+int inv_cta_lift(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sms,
+                 const vkcu_lift& lift);
+int poly_cta_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
+                  const vkcu_lift& lift);
 // cluster of 2^logc CTAs, n = 2^(14 + logc)
 int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
-int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
-int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc);
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,
+                const vkcu_lift* lift = nullptr);
+int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
+                 const vkcu_lift* lift = nullptr);
 
 template <class K>
 static int prepare(K kernel, int smem) {
@@ -566,6 +625,19 @@ static int grid_for(K kernel, int threads, int smem, long work, int sms) {
     default:                                                                  \
       if (variant != 0) { variant = 0; goto retry; }                          \
       return (int)cudaErrorInvalidValue;                                      \
+  }
+
+// Default shape of each degree (variant 0 above).
+#define VK_FOR_LOGN_DEFAULT(X)                                                \
+  switch (log_n) {                                                            \
+    case 8: return X(8, 16, 1);                                               \
+    case 9: return X(9, 16, 1);                                               \
+    case 10: return X(10, 16, 1);                                             \
+    case 11: return X(11, 16, 1);                                             \
+    case 12: return X(12, 16, 1);                                             \
+    case 13: return X(13, 32, 1);                                             \
+    case 14: return X(14, 32, 1);                                             \
+    default: return (int)cudaErrorInvalidValue;                               \
   }
 
 }  // namespace vk

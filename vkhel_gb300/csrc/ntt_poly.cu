@@ -12,7 +12,7 @@ static int launch(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const v
   static const int prepared = prepare(kern, S::SMEM_BYTES);
   if (prepared) return prepared;
   const int grid = grid_for(kern, S::T, S::SMEM_BYTES, (long)njobs, sms);
-  kern<<<grid, S::T, S::SMEM_BYTES, st>>>(jobs, njobs, one);
+  kern<<<grid, S::T, S::SMEM_BYTES, st>>>(jobs, njobs, one, vkcu_lift{});
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -1,0 +1,28 @@
+// Launcher of the CTA-resident fused polynomial multiplies with a fused
+// epilogue (the reference's centred-lift element-wise ops after the inverse
+// transform) for 2^8 <= n <= 2^14, default shape of each degree.
+#include "ntt_core.cuh"
+
+namespace vk {
+
+template <int LOGN, int E, int U>
+static int launch_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int sms,
+                       const vkcu_lift& lift) {
+  using S = Shape<LOGN, E, U>;
+  auto kern = k_polymul<LOGN, E, U, true>;
+  static const int prepared = prepare(kern, S::SMEM_BYTES);
+  if (prepared) return prepared;
+  const int grid = grid_for(kern, S::T, S::SMEM_BYTES, (long)njobs, sms);
+  kern<<<grid, S::T, S::SMEM_BYTES, st>>>(jobs, njobs, one, lift);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
+}
+
+int poly_cta_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
+                  const vkcu_lift& lift) {
+#define X(L, E, U) launch_lift<L, E, U>(st, jobs, njobs, one, sms, lift)
+  VK_FOR_LOGN_DEFAULT(X)
+#undef X
+}
+
+}  // namespace vk

@@ -151,6 +151,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 			if (nclasses == 0 || classes[nclasses - 1].log_n != log_n) {
 				struct vkh_job_class *cl = &classes[nclasses++];
 				cl->log_n = log_n;
+				cl->lift = 0;
 				cl->first = i;
 				cl->count = 0;
 				cl->fused = fused_log_n(log_n);
@@ -169,8 +170,8 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 			e = vkcu_stream_wait(s->s_comp, sl->ev_in);
 		if (!e)
 			e = s->forked ? vkh_issue_classes_forked(s->s_comp, s->aux, s->fork, s->join, ctx->sms, dpoly, dntt,
-					classes, nclasses)
-				: vkh_issue_classes(s->s_comp, ctx->sms, dpoly, dntt, classes, nclasses);
+					classes, nclasses, NULL)
+				: vkh_issue_classes(s->s_comp, ctx->sms, dpoly, dntt, classes, nclasses, NULL);
 		if (!e)
 			e = vkcu_event_record(sl->ev_comp, s->s_comp);
 		if (!e)
