@@ -182,6 +182,40 @@ uint32_t vkhel_batch_jobs(const struct vkhel_batch *batch);
 uint32_t vkhel_batch_kernels(const struct vkhel_batch *batch);
 void vkhel_batch_destroy(struct vkhel_batch *batch);
 
+/* ---- element-wise batch ----
+ * Many independent element-wise jobs of ragged lengths, each one of the
+ * reference's element-wise ops on its own vectors, run as one kernel launch
+ * (optionally replayed from a CUDA graph).  Each job gives exactly what the
+ * matching single call gives; jobs run concurrently, so commit rejects a
+ * batch in which a job writes memory that another job reads or writes (a job
+ * may work in place).  No counterpart in the reference. */
+enum vkhel_elem_op {
+	VKHEL_ELEM_FMA = 1,           /* p0 multiplier, p1 mod: vkhel_vector_elemfma */
+	VKHEL_ELEM_FMA_CANONICAL = 2, /* p0 multiplier, p1 mod: vkhel_vector_elemfma_canonical */
+	VKHEL_ELEM_MUL = 3,           /* p0 mod: vkhel_vector_elemmul */
+	VKHEL_ELEM_MULCONST = 4,      /* p0 multiplier, p1 mod: the inverse transform's
+	                               * n^-1 scaling kernel (src/vector.c:635-638) */
+	VKHEL_ELEM_MOD = 5,           /* p0 mod, p1 q: vkhel_vector_elemmod */
+	VKHEL_ELEM_GTADD = 6,         /* p0 bound, p1 diff: vkhel_vector_elemgtadd */
+	VKHEL_ELEM_GTSUB = 7          /* p0 bound, p1 diff, p2 mod: vkhel_vector_elemgtsub */
+};
+struct vkhel_elem_batch;
+struct vkhel_elem_batch *vkhel_elem_batch_create(struct vkhel_ctx *ctx);
+/* result->length words, as the single call; b is ignored by unary ops. */
+int vkhel_elem_batch_add(struct vkhel_elem_batch *batch, uint32_t op,
+		uint64_t p0, uint64_t p1, uint64_t p2, const struct vkhel_vector *a,
+		const struct vkhel_vector *b, struct vkhel_vector *result);
+/* Same on raw device pointers (8-byte aligned) of `len` words. */
+int vkhel_elem_batch_add_raw(struct vkhel_elem_batch *batch, uint32_t op,
+		uint64_t p0, uint64_t p1, uint64_t p2, const uint64_t *a,
+		const uint64_t *b, uint64_t *result, uint64_t len);
+/* flags: VKHEL_BATCH_GRAPH to capture the launch into a CUDA graph. */
+int vkhel_elem_batch_commit(struct vkhel_elem_batch *batch, uint32_t flags);
+int vkhel_elem_batch_launch(struct vkhel_elem_batch *batch);
+int vkhel_elem_batch_run(struct vkhel_elem_batch *batch);
+uint32_t vkhel_elem_batch_jobs(const struct vkhel_elem_batch *batch);
+void vkhel_elem_batch_destroy(struct vkhel_elem_batch *batch);
+
 /* ---- kernel variants (autotuning) ----
  * Each fused kernel family has, per degree 2^log_n, a few compiled variants
  * (threads per polynomial, radix-16 groups in flight per thread); the table

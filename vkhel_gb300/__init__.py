@@ -79,6 +79,14 @@ _SIGNATURES = [
     ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_lift", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp, vp, u32]),
+    ("vkhel_elem_batch_create", vp, [vp]),
+    ("vkhel_elem_batch_add", ctypes.c_int, [vp, u32, u64, u64, u64, vp, vp, vp]),
+    ("vkhel_elem_batch_add_raw", ctypes.c_int, [vp, u32, u64, u64, u64, vp, vp, vp, u64]),
+    ("vkhel_elem_batch_commit", ctypes.c_int, [vp, u32]),
+    ("vkhel_elem_batch_launch", ctypes.c_int, [vp]),
+    ("vkhel_elem_batch_run", ctypes.c_int, [vp]),
+    ("vkhel_elem_batch_jobs", u32, [vp]),
+    ("vkhel_elem_batch_destroy", None, [vp]),
     ("vkhel_batch_commit", ctypes.c_int, [vp, u32]),
     ("vkhel_batch_launch", ctypes.c_int, [vp]),
     ("vkhel_batch_run", ctypes.c_int, [vp]),
@@ -447,6 +455,60 @@ class Batch:
     def close(self):
         if getattr(self, "ptr", None) and getattr(self.ctx, "ptr", None):
             lib().vkhel_batch_destroy(self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+ELEM_OPS = {"elemfma": 1, "elemfma_canonical": 2, "elemmul": 3, "elemmulconst": 4, "elemmod": 5,
+            "elemgtadd": 6, "elemgtsub": 7}
+
+
+class ElemBatch:
+    """vkhel_elem_batch: independent element-wise jobs of ragged lengths in one launch."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.ptr = lib().vkhel_elem_batch_create(ctx.ptr)
+        if not self.ptr:
+            _check_ctx(ctx.ptr)
+        self._keep = []
+        ctx._children.add(self)
+
+    def add(self, op, a, b, res, *params):
+        """op name (elemfma, elemmod, ...) with the single call's parameters in order."""
+        p = [int(x) for x in params] + [0, 0, 0]
+        code = ELEM_OPS.get(op, op)
+        if isinstance(res, Vector):
+            self._keep.append((a, b, res))
+            rc = lib().vkhel_elem_batch_add(self.ptr, code, p[0], p[1], p[2], a.ptr, b.ptr if b is not None else None,
+                                            res.ptr)
+        else:  # (device pointer, length) for res; raw pointers for a and b
+            ptr, n = res
+            rc = lib().vkhel_elem_batch_add_raw(self.ptr, code, p[0], p[1], p[2], int(a),
+                                                int(b) if b is not None else None, int(ptr), int(n))
+        _status(self.ctx.ptr, rc)
+
+    def commit(self, graph=True):
+        _status(self.ctx.ptr, lib().vkhel_elem_batch_commit(self.ptr, BATCH_GRAPH if graph else 0))
+
+    def launch(self):
+        _status(self.ctx.ptr, lib().vkhel_elem_batch_launch(self.ptr))
+
+    def run(self):
+        _status(self.ctx.ptr, lib().vkhel_elem_batch_run(self.ptr))
+
+    @property
+    def jobs(self):
+        return lib().vkhel_elem_batch_jobs(self.ptr)
+
+    def close(self):
+        if getattr(self, "ptr", None) and getattr(self.ctx, "ptr", None):
+            lib().vkhel_elem_batch_destroy(self.ptr)
         self.ptr = None
 
     def __del__(self):

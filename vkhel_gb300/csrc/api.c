@@ -348,7 +348,7 @@ static int check_ops(const char *op, const struct vkhel_vector *a, const struct 
 	return VKHEL_OK;
 }
 
-static int check_mod(struct vkhel_ctx *ctx, const char *op, uint64_t mod) {
+int vkh_check_mod(struct vkhel_ctx *ctx, const char *op, uint64_t mod) {
 	/* Barrett needs bitlen(mod) + 62 >= 64 (include/priv/numbers.h:7-9) */
 	if (mod < 2)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "%s: modulus %" PRIu64 " < 2", op, mod);
@@ -364,7 +364,7 @@ static int finish(struct vkhel_ctx *ctx, int launch_err, const char *op) {
 
 void vkhel_vector_elemfma(const struct vkhel_vector *a, const struct vkhel_vector *b,
 		struct vkhel_vector *res, uint64_t multiplier, uint64_t mod) {
-	if (check_ops("elemfma", a, b, res, true) || check_mod(res->ctx, "elemfma", mod))
+	if (check_ops("elemfma", a, b, res, true) || vkh_check_mod(res->ctx, "elemfma", mod))
 		return;
 	/* elemfma.c:159-161: Shoup factor of the multiplier, truncated */
 	const uint64_t ms = vkh_shoup(multiplier, mod);
@@ -374,7 +374,7 @@ void vkhel_vector_elemfma(const struct vkhel_vector *a, const struct vkhel_vecto
 
 void vkhel_vector_elemfma_canonical(const struct vkhel_vector *a, const struct vkhel_vector *b,
 		struct vkhel_vector *res, uint64_t multiplier, uint64_t mod) {
-	if (check_ops("elemfma_canonical", a, b, res, true) || check_mod(res->ctx, "elemfma_canonical", mod))
+	if (check_ops("elemfma_canonical", a, b, res, true) || vkh_check_mod(res->ctx, "elemfma_canonical", mod))
 		return;
 	const uint64_t m = multiplier % mod;
 	finish(res->ctx,
@@ -402,14 +402,14 @@ void vkhel_vector_elemmod(const struct vkhel_vector *a, struct vkhel_vector *res
 		finish(res->ctx, vkcu_elemmodbytwo(res->ctx->stream, res->dev, a->dev, res->length, q / 2), "elemmod");
 		return;
 	}
-	if (check_mod(res->ctx, "elemmod", mod))
+	if (vkh_check_mod(res->ctx, "elemmod", mod))
 		return;
 	elemgtsub(res, a, q / 2, q, mod);
 }
 
 void vkhel_vector_elemmul(const struct vkhel_vector *a, const struct vkhel_vector *b,
 		struct vkhel_vector *res, uint64_t mod) {
-	if (check_ops("elemmul", a, b, res, true) || check_mod(res->ctx, "elemmul", mod))
+	if (check_ops("elemmul", a, b, res, true) || vkh_check_mod(res->ctx, "elemmul", mod))
 		return;
 	finish(res->ctx,
 			vkcu_elemmul(res->ctx->stream, res->dev, a->dev, b->dev, res->length, mod, vkh_barrett_mu(mod),
@@ -425,7 +425,7 @@ void vkhel_vector_elemgtadd(const struct vkhel_vector *a, struct vkhel_vector *r
 
 void vkhel_vector_elemgtsub(const struct vkhel_vector *a, struct vkhel_vector *res, uint64_t bound, uint64_t diff,
 		uint64_t mod) {
-	if (check_ops("elemgtsub", a, NULL, res, false) || check_mod(res->ctx, "elemgtsub", mod))
+	if (check_ops("elemgtsub", a, NULL, res, false) || vkh_check_mod(res->ctx, "elemgtsub", mod))
 		return;
 	elemgtsub(res, a, bound, diff, mod);
 }
@@ -524,7 +524,7 @@ int vkh_lift_compile(struct vkhel_ctx *ctx, const struct vkhel_lift_step *steps,
 				d->bound = qq / 2;
 				break;
 			}
-			const int st = check_mod(ctx, "lift elemmod", s->p0);
+			const int st = vkh_check_mod(ctx, "lift elemmod", s->p0);
 			if (st)
 				return st;
 			d->kind = VKCU_LIFT_GTSUB | tq;
@@ -536,7 +536,7 @@ int vkh_lift_compile(struct vkhel_ctx *ctx, const struct vkhel_lift_step *steps,
 			break;
 		}
 		case VKHEL_LIFT_ELEMGTSUB: {
-			const int st = check_mod(ctx, "lift elemgtsub", s->p2);
+			const int st = vkh_check_mod(ctx, "lift elemgtsub", s->p2);
 			if (st)
 				return st;
 			d->kind = VKCU_LIFT_GTSUB;

@@ -94,6 +94,31 @@ int vkcu_elemgtadd(void *stream, uint64_t *res, const uint64_t *a,
 int vkcu_elemmodbytwo(void *stream, uint64_t *res, const uint64_t *a,
 		uint64_t len, uint64_t signed_bound);
 
+/* One job of an element-wise batch: res[i] = op(a[i], b[i]) for i < len,
+ * with the op's constants as the single-vector launchers take them. */
+enum {
+	VKCU_ELEM_MUL = 1,        /* c0 mod, c1 mu, bits */
+	VKCU_ELEM_MULCONST = 2,   /* c0 c, c1 c_shoup, c2 mod */
+	VKCU_ELEM_FMA = 3,        /* c0 m, c1 m_shoup, c2 mod (reference wrap) */
+	VKCU_ELEM_FMA_CANON = 4,  /* c0 m mod q, c1 m_shoup, c2 mod, c3 mu, bits */
+	VKCU_ELEM_GTSUB = 5,      /* c0 bound, c1 reduced diff, c2 mod, c3 mu, bits */
+	VKCU_ELEM_GTADD = 6,      /* c0 bound, c1 diff */
+	VKCU_ELEM_MODTWO = 7      /* c0 signed bound */
+};
+typedef struct vkcu_elem_job {
+	uint32_t op, bits;
+	const uint64_t *a, *b;       /* b NULL for unary ops */
+	uint64_t *res;
+	uint64_t len;
+	uint64_t c0, c1, c2, c3;
+} vkcu_elem_job;
+/* Words per work unit of the element-wise batch kernel. */
+#define VKCU_ELEM_CHUNK 4096
+/* All jobs of a batch in one launch: `first` holds njobs + 1 prefix sums of
+ * the jobs' chunk counts (device memory, like `jobs`). */
+int vkcu_elem_batch(void *stream, const vkcu_elem_job *jobs, const uint64_t *first, uint32_t njobs,
+		uint64_t chunks, int sms);
+
 /* Device twiddle generation (q < 2^61, w^n = -1): fwd/inv are n interleaved
  * (root, shoup) pairs; phi[j] = w^(j 2^lb), plo[k] = w^k for k < 2^lb. */
 int vkcu_twiddles(void *stream, uint64_t *fwd, uint64_t *inv, const uint64_t *phi,
