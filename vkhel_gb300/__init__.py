@@ -487,10 +487,11 @@ class ElemBatch:
             self._keep.append((a, b, res))
             rc = lib().vkhel_elem_batch_add(self.ptr, code, p[0], p[1], p[2], a.ptr, b.ptr if b is not None else None,
                                             res.ptr)
-        else:  # (device pointer, length) for res; raw pointers for a and b
+        else:  # (device pointer, length) for res; device pointers (or vectors) for a and b
             ptr, n = res
-            rc = lib().vkhel_elem_batch_add_raw(self.ptr, code, p[0], p[1], p[2], int(a),
-                                                int(b) if b is not None else None, int(ptr), int(n))
+            dp = lambda x: None if x is None else (x.device_ptr if isinstance(x, Vector) else int(x))
+            self._keep.append((a, b))
+            rc = lib().vkhel_elem_batch_add_raw(self.ptr, code, p[0], p[1], p[2], dp(a), dp(b), int(ptr), int(n))
         _status(self.ctx.ptr, rc)
 
     def commit(self, graph=True):
