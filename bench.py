@@ -327,7 +327,133 @@ def extra_configs(vk, torch):
                            "limb_polymul_per_s": limbs_total / sec, "gmodmul_per_s": modmuls / sec / 1e9,
                            "kernels_per_batch": kernels}
     del jobs
+    out["lift_epilogue"] = lift_epilogue(vk, ctx, torch, orc)
+    out["elementwise_batch"] = elementwise_batch(vk, ctx, torch, orc)
+    out["device_twiddles"] = device_twiddles(vk, ctx, torch)
     ctx.close()
+    return out
+
+
+def _event_time(torch, ctx, fn, reps):
+    """Seconds per call of fn() (asynchronous launches on the context stream)."""
+    st = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(3):
+        fn()
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        fn()
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3 / reps
+
+
+def lift_epilogue(vk, ctx, torch, orc, pairs=4 * PAIRS):
+    """The rns_batch polynomials (n = 16384, 8 limbs, seed 2), 128 pairs so
+    that the 384 MB of operands exceed L2, with and without a fused BFV-style
+    centred reduction mod t = 65537 of every limb (elemmod(t, q_limb) after
+    the inverse transform): the epilogue's cost."""
+    from vkhel_gb300 import workloads
+    qs, ws, a, b = workloads.rns_batch(N, LIMBS, pairs, SEED)
+    tabs = [vk.NttTables(N, q, w) for q, w in zip(qs, ws)]
+    pa = [vk.Vector(ctx, a[i].reshape(-1)) for i in range(pairs)]
+    pb = [vk.Vector(ctx, b[i].reshape(-1)) for i in range(pairs)]
+    pc = [vk.Vector(ctx, LIMBS * N) for _ in range(pairs)]
+    rates = {}
+    for name, lift in (("plain", None), ("lift", [("elemmod", 65537, 0)])):
+        bt = vk.Batch(ctx)
+        for i in range(pairs):
+            bt.add_polymul(tabs, pa[i], pb[i], pc[i], lift=lift)
+        bt.commit(graph=True)
+        rates[name] = pairs * LIMBS / _event_time(torch, ctx, bt.launch, 20)
+        bt.close()
+    ref, _ = orc.polymul(a[0, 1], b[0, 1], N, qs[1], ws[1])
+    ref = orc.elemmod(ref, 65537, qs[1])
+    assert np.array_equal(pc[0].download()[N:2 * N], ref), "lifted product differs from the oracle"
+    return {"workload": f"n={N}, {LIMBS} limbs, {pairs} pairs, seed {SEED}; epilogue elemmod(t=65537, q of each limb)",
+            "limb_polymul_per_s_plain": rates["plain"], "limb_polymul_per_s_lift": rates["lift"],
+            "epilogue_cost_frac": 1 - rates["lift"] / rates["plain"]}
+
+
+def elementwise_batch(vk, ctx, torch, orc, jobs=2048, seed=6):
+    """2048 ragged element-wise jobs (lengths uniform in 1 .. 2^17 words, ops
+    cycling through elemfma, elemmul, elemmod, elemgtsub, elemgtadd, 61-bit
+    modulus, seed 6) as one launch: GB/s of operand traffic against the HBM
+    copy peak, and the same jobs as single blocking calls."""
+    from vkhel_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    q = (1 << 61) - 1
+    ops = [("elemfma", (123456789, q), True), ("elemmul", (q,), True), ("elemmod", (65537, q), False),
+           ("elemgtsub", (q // 2, q, 1 << 40), False), ("elemgtadd", (q // 2, 12345), False)]
+    lens = rng.integers(1, 1 << 17, size=jobs)
+    total = int(lens.sum())
+    pool_a = vk.Vector(ctx, workloads.uniform(rng, q, total))
+    pool_b = vk.Vector(ctx, workloads.uniform(rng, q, total))
+    pool_r = vk.Vector(ctx, total)
+    eb = vk.ElemBatch(ctx)
+    off, nbytes, spans = 0, 0, []
+    for j, n in enumerate(lens.tolist()):
+        op, params, binary = ops[j % len(ops)]
+        eb.add(op, pool_a.device_ptr + 8 * off, pool_b.device_ptr + 8 * off if binary else None,
+               (pool_r.device_ptr + 8 * off, n), *params)
+        nbytes += n * (24 if binary else 16)
+        spans.append((off, n, op, params))
+        off += n
+    eb.commit(graph=True)
+    sec = _event_time(torch, ctx, eb.launch, 20)
+    got = pool_r.download()
+    a_h, b_h = pool_a.download(), pool_b.download()
+    for off, n, op, params in spans[:5]:
+        x, y = a_h[off:off + n], b_h[off:off + n]
+        ref = {"elemfma": lambda: orc.elemfma(x, y, *params), "elemmul": lambda: orc.elemmul(x, y, *params),
+               "elemmod": lambda: orc.elemmod(x, *params), "elemgtsub": lambda: orc.elemgtsub(x, *params),
+               "elemgtadd": lambda: orc.elemgtadd(x, *params)}[op]()
+        assert np.array_equal(got[off:off + n], ref), f"element-wise batch job {op} differs from the oracle"
+    # the same jobs as the reference's blocking single calls (first 64 jobs)
+    sub = spans[:64]
+    vecs = [(vk.Vector(ctx, a_h[o:o + n]), vk.Vector(ctx, b_h[o:o + n]), vk.Vector(ctx, n), op, p)
+            for o, n, op, p in sub]
+    t0 = time.perf_counter()
+    for va, vb, vr, op, p in vecs:
+        if op in ("elemfma", "elemmul"):
+            getattr(vk, op)(va, vb, vr, *p)
+        else:
+            getattr(vk, op)(va, vr, *p)
+    single = (time.perf_counter() - t0) / len(sub)
+    peaks, src = load_peaks()
+    gbs = nbytes / sec / 1e9
+    eb.close()
+    return {"workload": f"{jobs} jobs, lengths uniform in 1..2^17 words ({total} words), 5 ops cycling, "
+                        f"61-bit modulus, seed {seed}",
+            "ms_per_batch": sec * 1e3, "jobs_per_s": jobs / sec, "gbs": gbs, "bytes_per_batch": nbytes,
+            "hbm_peak_gbs": peaks.get("hbm_gbs"), "hbm_frac": gbs / peaks.get("hbm_gbs", 6800.0),
+            "peak_source": src, "kernels_per_batch": 1,
+            "single_call_jobs_per_s": 1 / single, "speedup_vs_single_calls": (jobs / sec) * single}
+
+
+def device_twiddles(vk, ctx, torch):
+    """Set-up time of the device twiddle tables for n = 2^17: generated on the
+    GPU (60-bit prime) against built on the host and uploaded (62-bit prime,
+    outside the device generator's range), each measured as the first
+    forward transform's extra time over a second one."""
+    from vkhel_gb300 import workloads
+    n = 1 << 17
+    out = {"workload": f"n = {n}, forward transform of one vector"}
+    for name, bound in (("device_generated", 1 << 60), ("host_built", 1 << 62)):
+        q = workloads.ntt_primes(n, 1, bound=bound)[0]
+        w = workloads.root_for(n, q)
+        v = vk.Vector(ctx, n)
+        ctx.sync()
+        t0 = time.perf_counter()
+        t = vk.NttTables(n, q, w)
+        vk.forward_transform(v, v, t)
+        first = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        vk.forward_transform(v, v, t)
+        second = time.perf_counter() - t0
+        out[name + "_setup_ms"] = (first - second) * 1e3
+        out[name + "_q_bits"] = q.bit_length()
     return out
 
 
