@@ -108,7 +108,7 @@ def test_batch_replays_read_fresh_operands(vk, ctx, oracle):
 
 def test_commit_rejects_dependent_jobs(vk, ctx):
     n = 1000
-    x, y, z = vk.Vector(ctx, 2 * n), vk.Vector(ctx, n), vk.Vector(ctx, n)
+    x, y, z, u = vk.Vector(ctx, 2 * n), vk.Vector(ctx, n), vk.Vector(ctx, n), vk.Vector(ctx, n)
     # writes overlap
     eb = vk.ElemBatch(ctx)
     eb.add("elemgtadd", y, None, (x.device_ptr, n), 1, 1)
@@ -118,7 +118,7 @@ def test_commit_rejects_dependent_jobs(vk, ctx):
     # one job reads what another writes
     eb = vk.ElemBatch(ctx)
     eb.add("elemmod", y, None, z, 3, Q)
-    eb.add("elemmul", z, y, x, Q)
+    eb.add("elemmul", z, y, u, Q)
     with pytest.raises(vk.VkhelError):
         eb.commit()
     # in place and disjoint halves are fine
