@@ -13,6 +13,7 @@
  * batches.  A job may work in place (res equal to one of its operands).
  */
 #include <inttypes.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -23,10 +24,10 @@ struct vkhel_elem_batch {
 	vkcu_elem_job *jobs;
 	uint32_t njobs, cap;
 	int committed;
-	void *dev;              /* jobs, then njobs + 1 chunk prefix sums */
+	void *dev;              /* jobs, then the chunk table */
 	uint64_t dev_bytes;
 	vkcu_elem_job *dev_jobs;
-	uint64_t *dev_first;
+	vkcu_elem_chunk *dev_chunks;
 	uint64_t chunks;
 	void *graph;
 };
@@ -224,18 +225,26 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 	if (dep)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT,
 				"elem_batch_commit: job %u overlaps memory another job writes", bad);
+	uint64_t chunks = 0;
+	for (uint32_t i = 0; i < b->njobs; i++) {
+		const uint64_t c = (b->jobs[i].len + VKCU_ELEM_CHUNK - 1) / VKCU_ELEM_CHUNK;
+		if (c > UINT32_MAX)
+			return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "elem_batch_commit: job %u too long", i);
+		chunks += c;
+	}
 	const uint64_t job_bytes = sizeof(vkcu_elem_job) * b->njobs;
-	const uint64_t first_off = (job_bytes + 255) & ~(uint64_t) 255;
-	b->dev_bytes = first_off + sizeof(uint64_t) * ((uint64_t) b->njobs + 1);
+	const uint64_t chunk_off = (job_bytes + 255) & ~(uint64_t) 255;
+	b->dev_bytes = chunk_off + sizeof(vkcu_elem_chunk) * (chunks ? chunks : 1);
 	char *host = malloc(b->dev_bytes);
 	if (!host)
 		return vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "elem_batch_commit: host allocation failed");
 	memcpy(host, b->jobs, job_bytes);
-	uint64_t *first = (uint64_t *) (host + first_off);
-	first[0] = 0;
+	vkcu_elem_chunk *table = (vkcu_elem_chunk *) (host + chunk_off);
+	uint64_t k = 0;
 	for (uint32_t i = 0; i < b->njobs; i++)
-		first[i + 1] = first[i] + (b->jobs[i].len + VKCU_ELEM_CHUNK - 1) / VKCU_ELEM_CHUNK;
-	b->chunks = first[b->njobs];
+		for (uint64_t c = 0; c * VKCU_ELEM_CHUNK < b->jobs[i].len; c++)
+			table[k++] = (vkcu_elem_chunk){i, (uint32_t) c};
+	b->chunks = chunks;
 	int st = vkh_dev_alloc(ctx, b->dev_bytes, &b->dev);
 	if (st) {
 		free(host);
@@ -248,11 +257,11 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 	if (e)
 		return vkh_cuda(ctx, e, "elem_batch_commit: job table upload");
 	b->dev_jobs = b->dev;
-	b->dev_first = (uint64_t *) ((char *) b->dev + first_off);
+	b->dev_chunks = (vkcu_elem_chunk *) ((char *) b->dev + chunk_off);
 	if ((flags & VKHEL_BATCH_GRAPH) && b->chunks) {
 		e = vkcu_capture_begin(ctx->stream);
 		if (!e) {
-			const int ie = vkcu_elem_batch(ctx->stream, b->dev_jobs, b->dev_first, b->njobs, b->chunks, ctx->sms);
+			const int ie = vkcu_elem_batch(ctx->stream, b->dev_jobs, b->dev_chunks, b->chunks, ctx->sms);
 			void *exec = NULL;
 			e = vkcu_capture_end(ctx->stream, &exec);
 			if (!e)
@@ -277,7 +286,7 @@ int vkhel_elem_batch_launch(struct vkhel_elem_batch *b) {
 		if (!e)
 			vkcu_count_launches(1);
 	} else if (b->chunks) {
-		e = vkcu_elem_batch(b->ctx->stream, b->dev_jobs, b->dev_first, b->njobs, b->chunks, b->ctx->sms);
+		e = vkcu_elem_batch(b->ctx->stream, b->dev_jobs, b->dev_chunks, b->chunks, b->ctx->sms);
 	}
 	return vkh_cuda(b->ctx, e, "elem_batch_launch");
 }

@@ -114,10 +114,14 @@ typedef struct vkcu_elem_job {
 } vkcu_elem_job;
 /* Words per work unit of the element-wise batch kernel. */
 #define VKCU_ELEM_CHUNK 4096
-/* All jobs of a batch in one launch: `first` holds njobs + 1 prefix sums of
- * the jobs' chunk counts (device memory, like `jobs`). */
-int vkcu_elem_batch(void *stream, const vkcu_elem_job *jobs, const uint64_t *first, uint32_t njobs,
-		uint64_t chunks, int sms);
+/* Work unit: words [chunk * VKCU_ELEM_CHUNK, +VKCU_ELEM_CHUNK) of job `job`. */
+typedef struct vkcu_elem_chunk {
+	uint32_t job, chunk;
+} vkcu_elem_chunk;
+/* All jobs of a batch in one launch over `nchunks` work units (device
+ * memory, like `jobs`). */
+int vkcu_elem_batch(void *stream, const vkcu_elem_job *jobs, const vkcu_elem_chunk *chunks, uint64_t nchunks,
+		int sms);
 
 /* Device twiddle generation (q < 2^61, w^n = -1): fwd/inv are n interleaved
  * (root, shoup) pairs; phi[j] = w^(j 2^lb), plo[k] = w^k for k < 2^lb. */
