@@ -329,7 +329,7 @@ def extra_configs(vk, torch):
     del jobs
     out["lift_epilogue"] = lift_epilogue(vk, ctx, torch, orc)
     out["elementwise_batch"] = elementwise_batch(vk, ctx, torch, orc)
-    out["device_twiddles"] = device_twiddles(vk, ctx, torch)
+    out["device_twiddles"] = device_twiddles(vk, ctx, torch, orc)
     ctx.close()
     return out
 
@@ -432,7 +432,7 @@ def elementwise_batch(vk, ctx, torch, orc, jobs=2048, seed=6):
             "single_call_jobs_per_s": 1 / single, "speedup_vs_single_calls": (jobs / sec) * single}
 
 
-def device_twiddles(vk, ctx, torch):
+def device_twiddles(vk, ctx, torch, orc=None):
     """Set-up time of the device twiddle tables for n = 2^17: generated on the
     GPU (60-bit prime) against built on the host and uploaded (62-bit prime,
     outside the device generator's range), each measured as the first
@@ -457,6 +457,10 @@ def device_twiddles(vk, ctx, torch):
     return out
 
 
+EXTRAS = {"lift_epilogue": lift_epilogue, "elementwise_batch": elementwise_batch,
+          "device_twiddles": device_twiddles}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,6 +471,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
     ap.add_argument("--profile", action="store_true",
                     help="small profiling case: build the batch, launch it --steps times, print nothing else")
+    ap.add_argument("--extra", choices=sorted(EXTRAS),
+                    help="run one of the secondary measurements alone and print its JSON (profiling aid)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -483,6 +489,11 @@ def main():
     import vkhel_gb300 as vk
     from oracle import pyoracle
     from vkhel_gb300 import workloads
+    if args.extra:
+        ctx = vk.Context()
+        print(json.dumps({args.extra: EXTRAS[args.extra](vk, ctx, torch, pyoracle.load())}), flush=True)
+        ctx.close()
+        return
     # Two contexts = two streams: consecutive independent batches overlap, so
     # the second wave of one batch (256 jobs on 152 SMs) shares the GPU with
     # the first wave of the next, as in a continuous stream of batches.

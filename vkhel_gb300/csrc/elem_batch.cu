@@ -2,13 +2,14 @@
 // lengths (each one of the reference's element-wise ops with its own
 // operands and constants) in one launch.
 //
-// Work is cut into chunks of VKCU_ELEM_CHUNK words listed in a chunk table
-// (job, chunk index) built at commit; a persistent grid (one wave) walks
-// the table, fetching the next chunk's descriptor while the current chunk
-// streams, with 16-byte accesses where the job's three pointers are 16-byte
-// aligned (8-byte otherwise; a full aligned chunk issues all of a thread's
-// loads before its stores).  The op is uniform per chunk, so the switch costs
-// one branch per chunk.  HBM-bound: 16 (unary) or 24 (binary) bytes per word.
+// At commit every job is cut into units of at most VKCU_ELEM_CHUNK words
+// (VKCU_ELEM_CHUNK_UNARY for unary ops, which move 16 instead of 24 bytes a
+// word), each a complete descriptor (pointers offset to the unit); a
+// persistent grid (one wave) walks the unit table with 16-byte accesses
+// where the unit's three pointers share their offset mod 16 (8-byte
+// otherwise), every load of a thread's group issued before its stores.  The op is uniform per unit,
+// so the switch costs one branch per unit.  HBM-bound: 16 (unary) or 24
+// (binary) bytes per word, plus 72 descriptor bytes per unit.
 #include <cuda_runtime.h>
 
 #include "elem_ops.cuh"
@@ -17,89 +18,106 @@
 namespace vk {
 
 constexpr int kThreads = 256;
-constexpr int kPairs = VKCU_ELEM_CHUNK / (2 * kThreads);  // 16-byte pairs per thread in a full chunk
+// 16-byte pairs of each operand per thread and group: one full unit per group
+constexpr int kPairsBinary = VKCU_ELEM_CHUNK / (2 * kThreads);
+constexpr int kPairsUnary = VKCU_ELEM_CHUNK_UNARY / (2 * kThreads);
+static_assert(kPairsBinary * 2 == kPairsUnary, "unary units move the bytes of binary ones");
 
-template <class Op>
-__device__ __forceinline__ void run_chunk(const vkcu_elem_job& j, u64 lo, u64 hi, const Op& op) {
+// One unit of `n` words.  Where a, b and res share their offset mod 16 bytes
+// (all aligned, or all 8 bytes off: one word is peeled), the words stream as
+// 16-byte pairs, otherwise as single words; either way in groups of
+// kThreads x P pairs (or words) with every load of a thread's group issued
+// before its first store.  Lanes past the end re-read the last element (no
+// conditionally defined registers) and store nothing.
+template <int P, bool BIN, class Op>
+__device__ __forceinline__ void run_chunk(const vkcu_elem_job& j, const Op& op) {
   const u64* a = reinterpret_cast<const u64*>(j.a);
   const u64* b = reinterpret_cast<const u64*>(j.b);
   u64* res = reinterpret_cast<u64*>(j.res);
-  const bool vec = ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
-                     reinterpret_cast<uintptr_t>(res)) & 15) == 0;
-  if (vec && hi - lo == VKCU_ELEM_CHUNK) {
-    // full chunk: every load of the thread in flight before the first store
-    ulonglong2 x[kPairs], y[kPairs];
+  const u64 n = j.len;
+  const uintptr_t ma = reinterpret_cast<uintptr_t>(a) & 15, mr = reinterpret_cast<uintptr_t>(res) & 15;
+  const bool same = ma == mr && (!BIN || (reinterpret_cast<uintptr_t>(b) & 15) == ma);
+  if (same) {
+    u64 s = 0;
+    if (ma && n) {  // peel one word to reach the 16-byte boundary
+      if (threadIdx.x == 0) res[0] = op(a[0], BIN ? b[0] : 0ull);
+      s = 1;
+    }
+    const u64 pairs = (n - s) >> 1;
+    for (u64 g0 = 0; g0 < pairs; g0 += (u64)kThreads * P) {
+      ulonglong2 x[P], y[BIN ? P : 1];
 #pragma unroll
-    for (int k = 0; k < kPairs; k++) {
-      const u64 i = lo + 2 * (threadIdx.x + (u64)k * kThreads);
-      x[k] = ld2(a + i);
-      y[k] = b ? ld2(b + i) : make_ulonglong2(0, 0);
-    }
+      for (int k = 0; k < P; k++) {
+        const u64 p = g0 + threadIdx.x + (u64)k * kThreads;
+        const u64 pc = p < pairs ? p : pairs - 1;
+        x[k] = ld2(a + s + 2 * pc);
+        if constexpr (BIN) y[k] = ld2(b + s + 2 * pc);
+      }
 #pragma unroll
-    for (int k = 0; k < kPairs; k++) {
-      const u64 i = lo + 2 * (threadIdx.x + (u64)k * kThreads);
-      st2(res + i, op(x[k].x, y[k].x), op(x[k].y, y[k].y));
+      for (int k = 0; k < P; k++) {
+        const u64 p = g0 + threadIdx.x + (u64)k * kThreads;
+        const ulonglong2 yk = BIN ? y[BIN ? k : 0] : make_ulonglong2(0, 0);
+        if (p < pairs) st2(res + s + 2 * p, op(x[k].x, yk.x), op(x[k].y, yk.y));
+      }
     }
-  } else if (vec) {
-    // lo is a multiple of the (even) chunk size: pairs start 16-byte aligned
-    const u64 pairs_end = lo + ((hi - lo) & ~1ull);
-#pragma unroll 4
-    for (u64 i = lo + 2 * threadIdx.x; i < pairs_end; i += 2 * kThreads) {
-      const ulonglong2 xv = ld2(a + i);
-      const ulonglong2 yv = b ? ld2(b + i) : make_ulonglong2(0, 0);
-      st2(res + i, op(xv.x, yv.x), op(xv.y, yv.y));
-    }
-    if (pairs_end < hi && threadIdx.x == 0) res[pairs_end] = op(a[pairs_end], b ? b[pairs_end] : 0ull);
+    const u64 last = s + 2 * pairs;
+    if (last < n && threadIdx.x == 0) res[last] = op(a[last], BIN ? b[last] : 0ull);
   } else {
-#pragma unroll 4
-    for (u64 i = lo + threadIdx.x; i < hi; i += kThreads) res[i] = op(a[i], b ? b[i] : 0ull);
-  }
-}
-
-__device__ __forceinline__ void run_job_chunk(const vkcu_elem_job& j, u32 chunk) {
-  const u64 w0 = (u64)chunk * VKCU_ELEM_CHUNK;
-  const u64 w1 = w0 + VKCU_ELEM_CHUNK < j.len ? w0 + VKCU_ELEM_CHUNK : j.len;
-  switch (j.op) {
-    case VKCU_ELEM_MUL: run_chunk(j, w0, w1, OpMul{j.c0, j.c1, j.bits}); break;
-    case VKCU_ELEM_MULCONST: run_chunk(j, w0, w1, OpMulConst{j.c0, j.c1, j.c2}); break;
-    case VKCU_ELEM_FMA: run_chunk(j, w0, w1, OpFmaRef{j.c0, j.c1, j.c2}); break;
-    case VKCU_ELEM_FMA_CANON: run_chunk(j, w0, w1, OpFmaCanon{j.c0, j.c1, j.c2, j.c3, j.bits}); break;
-    case VKCU_ELEM_GTSUB: run_chunk(j, w0, w1, OpGtSub{j.c0, j.c1, j.c2, j.c3, j.bits}); break;
-    case VKCU_ELEM_GTADD: run_chunk(j, w0, w1, OpGtAdd{j.c0, j.c1}); break;
-    default: run_chunk(j, w0, w1, OpModTwo{j.c0}); break;
-  }
-}
-
-// Persistent loop over the work units; the next unit's descriptor is fetched
-// before the current one streams, so its latency hides behind the stream.
-__global__ void __launch_bounds__(kThreads) k_elem_batch(const vkcu_elem_job* __restrict__ jobs,
-                                                         const vkcu_elem_chunk* __restrict__ chunks, u64 nchunks) {
-  u64 c = blockIdx.x;
-  if (c >= nchunks) return;
-  vkcu_elem_chunk cu = chunks[c];
-  vkcu_elem_job j = jobs[cu.job];
-  for (;;) {
-    const u64 cn = c + gridDim.x;
-    vkcu_elem_chunk nu = cu;
-    vkcu_elem_job nj = j;
-    if (cn < nchunks) {
-      nu = chunks[cn];
-      nj = jobs[nu.job];
+    for (u64 g0 = 0; g0 < n; g0 += (u64)kThreads * P) {
+      u64 x[P], y[BIN ? P : 1];
+#pragma unroll
+      for (int k = 0; k < P; k++) {
+        const u64 i = g0 + threadIdx.x + (u64)k * kThreads;
+        const u64 ic = i < n ? i : n - 1;
+        x[k] = a[ic];
+        if constexpr (BIN) y[k] = b[ic];
+      }
+#pragma unroll
+      for (int k = 0; k < P; k++) {
+        const u64 i = g0 + threadIdx.x + (u64)k * kThreads;
+        if (i < n) res[i] = op(x[k], BIN ? y[BIN ? k : 0] : 0ull);
+      }
     }
-    run_job_chunk(j, cu.chunk);
-    if (cn >= nchunks) break;
-    c = cn;
-    cu = nu;
-    j = nj;
+  }
+}
+
+template <class Op>
+__device__ __forceinline__ void run_binary(const vkcu_elem_job& j, const Op& op) {
+  run_chunk<kPairsBinary, true>(j, op);
+}
+
+template <class Op>
+__device__ __forceinline__ void run_unary(const vkcu_elem_job& j, const Op& op) {
+  run_chunk<kPairsUnary, false>(j, op);
+}
+
+__device__ __forceinline__ void run_unit(const vkcu_elem_job& j) {
+  switch (j.op) {
+    case VKCU_ELEM_MUL: run_binary(j, OpMul{j.c0, j.c1, j.bits}); break;
+    case VKCU_ELEM_FMA: run_binary(j, OpFmaRef{j.c0, j.c1, j.c2}); break;
+    case VKCU_ELEM_FMA_CANON: run_binary(j, OpFmaCanon{j.c0, j.c1, j.c2, j.c3, j.bits}); break;
+    case VKCU_ELEM_MULCONST: run_unary(j, OpMulConst{j.c0, j.c1, j.c2}); break;
+    case VKCU_ELEM_GTSUB: run_unary(j, OpGtSub{j.c0, j.c1, j.c2, j.c3, j.bits}); break;
+    case VKCU_ELEM_GTADD: run_unary(j, OpGtAdd{j.c0, j.c1}); break;
+    default: run_unary(j, OpModTwo{j.c0}); break;
+  }
+}
+
+// Persistent loop over the work units.  Four CTAs per SM (64 registers a
+// thread) keep more bytes in flight than fewer, larger CTAs that prefetch the
+// next unit's descriptor (measured on GB300: 5.4 against 4.7-5.1 TB/s).
+__global__ void __launch_bounds__(kThreads, 4) k_elem_batch(const vkcu_elem_job* __restrict__ units, u64 nunits) {
+  for (u64 c = blockIdx.x; c < nunits; c += gridDim.x) {
+    const vkcu_elem_job j = units[c];
+    run_unit(j);
   }
 }
 
 }  // namespace vk
 
-extern "C" int vkcu_elem_batch(void* stream, const vkcu_elem_job* jobs, const vkcu_elem_chunk* chunks,
-                               uint64_t nchunks, int sms) {
+extern "C" int vkcu_elem_batch(void* stream, const vkcu_elem_job* units, uint64_t nchunks, int sms) {
   if (nchunks == 0) return 0;
-  if (!jobs || !chunks) return (int)cudaErrorInvalidValue;
+  if (!units) return (int)cudaErrorInvalidValue;
   // one wave of resident CTAs: the loop is persistent
   static const int per_sm = [] {
     int b = 0;
@@ -109,7 +127,7 @@ extern "C" int vkcu_elem_batch(void* stream, const vkcu_elem_job* jobs, const vk
   }();
   const uint64_t cap = (uint64_t)(sms > 0 ? sms : 1) * per_sm;
   const uint64_t blocks = nchunks < cap ? nchunks : cap;
-  vk::k_elem_batch<<<(unsigned)blocks, vk::kThreads, 0, (cudaStream_t)stream>>>(jobs, chunks, nchunks);
+  vk::k_elem_batch<<<(unsigned)blocks, vk::kThreads, 0, (cudaStream_t)stream>>>(units, nchunks);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -24,10 +24,8 @@ struct vkhel_elem_batch {
 	vkcu_elem_job *jobs;
 	uint32_t njobs, cap;
 	int committed;
-	void *dev;              /* jobs, then the chunk table */
+	void *dev;              /* unit table: the jobs cut into VKCU_ELEM_CHUNK-word pieces */
 	uint64_t dev_bytes;
-	vkcu_elem_job *dev_jobs;
-	vkcu_elem_chunk *dev_chunks;
 	uint64_t chunks;
 	void *graph;
 };
@@ -227,23 +225,26 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 				"elem_batch_commit: job %u overlaps memory another job writes", bad);
 	uint64_t chunks = 0;
 	for (uint32_t i = 0; i < b->njobs; i++) {
-		const uint64_t c = (b->jobs[i].len + VKCU_ELEM_CHUNK - 1) / VKCU_ELEM_CHUNK;
-		if (c > UINT32_MAX)
-			return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "elem_batch_commit: job %u too long", i);
-		chunks += c;
+		const uint64_t unit = b->jobs[i].b ? VKCU_ELEM_CHUNK : VKCU_ELEM_CHUNK_UNARY;
+		chunks += (b->jobs[i].len + unit - 1) / unit;
 	}
-	const uint64_t job_bytes = sizeof(vkcu_elem_job) * b->njobs;
-	const uint64_t chunk_off = (job_bytes + 255) & ~(uint64_t) 255;
-	b->dev_bytes = chunk_off + sizeof(vkcu_elem_chunk) * (chunks ? chunks : 1);
-	char *host = malloc(b->dev_bytes);
+	b->dev_bytes = sizeof(vkcu_elem_job) * (chunks ? chunks : 1);
+	vkcu_elem_job *host = malloc(b->dev_bytes);
 	if (!host)
 		return vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "elem_batch_commit: host allocation failed");
-	memcpy(host, b->jobs, job_bytes);
-	vkcu_elem_chunk *table = (vkcu_elem_chunk *) (host + chunk_off);
 	uint64_t k = 0;
-	for (uint32_t i = 0; i < b->njobs; i++)
-		for (uint64_t c = 0; c * VKCU_ELEM_CHUNK < b->jobs[i].len; c++)
-			table[k++] = (vkcu_elem_chunk){i, (uint32_t) c};
+	for (uint32_t i = 0; i < b->njobs; i++) {
+		const vkcu_elem_job *j = &b->jobs[i];
+		const uint64_t unit = j->b ? VKCU_ELEM_CHUNK : VKCU_ELEM_CHUNK_UNARY;
+		for (uint64_t w = 0; w < j->len; w += unit) {
+			vkcu_elem_job u = *j;
+			u.a = j->a + w;
+			u.b = j->b ? j->b + w : NULL;
+			u.res = j->res + w;
+			u.len = j->len - w < unit ? j->len - w : unit;
+			host[k++] = u;
+		}
+	}
 	b->chunks = chunks;
 	int st = vkh_dev_alloc(ctx, b->dev_bytes, &b->dev);
 	if (st) {
@@ -255,13 +256,11 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 		e = vkcu_sync(ctx->stream);
 	free(host);
 	if (e)
-		return vkh_cuda(ctx, e, "elem_batch_commit: job table upload");
-	b->dev_jobs = b->dev;
-	b->dev_chunks = (vkcu_elem_chunk *) ((char *) b->dev + chunk_off);
+		return vkh_cuda(ctx, e, "elem_batch_commit: unit table upload");
 	if ((flags & VKHEL_BATCH_GRAPH) && b->chunks) {
 		e = vkcu_capture_begin(ctx->stream);
 		if (!e) {
-			const int ie = vkcu_elem_batch(ctx->stream, b->dev_jobs, b->dev_chunks, b->chunks, ctx->sms);
+			const int ie = vkcu_elem_batch(ctx->stream, b->dev, b->chunks, ctx->sms);
 			void *exec = NULL;
 			e = vkcu_capture_end(ctx->stream, &exec);
 			if (!e)
@@ -286,7 +285,7 @@ int vkhel_elem_batch_launch(struct vkhel_elem_batch *b) {
 		if (!e)
 			vkcu_count_launches(1);
 	} else if (b->chunks) {
-		e = vkcu_elem_batch(b->ctx->stream, b->dev_jobs, b->dev_chunks, b->chunks, b->ctx->sms);
+		e = vkcu_elem_batch(b->ctx->stream, b->dev, b->chunks, b->ctx->sms);
 	}
 	return vkh_cuda(b->ctx, e, "elem_batch_launch");
 }

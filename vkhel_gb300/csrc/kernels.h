@@ -112,16 +112,13 @@ typedef struct vkcu_elem_job {
 	uint64_t len;
 	uint64_t c0, c1, c2, c3;
 } vkcu_elem_job;
-/* Words per work unit of the element-wise batch kernel. */
-#define VKCU_ELEM_CHUNK 4096
-/* Work unit: words [chunk * VKCU_ELEM_CHUNK, +VKCU_ELEM_CHUNK) of job `job`. */
-typedef struct vkcu_elem_chunk {
-	uint32_t job, chunk;
-} vkcu_elem_chunk;
-/* All jobs of a batch in one launch over `nchunks` work units (device
- * memory, like `jobs`). */
-int vkcu_elem_batch(void *stream, const vkcu_elem_job *jobs, const vkcu_elem_chunk *chunks, uint64_t nchunks,
-		int sms);
+/* Words per work unit of the element-wise batch kernel: a batch is launched
+ * as a table of units, each a vkcu_elem_job of at most this many words (the
+ * jobs cut into pieces, pointers offset to each piece); unary ops take units
+ * twice as long, so that every unit moves the same bytes. */
+#define VKCU_ELEM_CHUNK 2048
+#define VKCU_ELEM_CHUNK_UNARY 4096
+int vkcu_elem_batch(void *stream, const vkcu_elem_job *units, uint64_t nunits, int sms);
 
 /* Device twiddle generation (q < 2^61, w^n = -1): fwd/inv are n interleaved
  * (root, shoup) pairs; phi[j] = w^(j 2^lb), plo[k] = w^k for k < 2^lb. */
