@@ -1,4 +1,4 @@
-"""Every compiled kernel variant is bit-exact.
+"""Every compiled kernel variant is bit-exact (with and without an epilogue).
 
 The autotuner only chooses among variants (words per thread, radix-16 groups
 in flight per thread, concurrent degree classes), so each variant of each
@@ -25,6 +25,7 @@ def test_every_variant_matches_oracle(vk, ctx, oracle, log_n):
     a_h, b_h = workloads.uniform(rng, q, n), workloads.uniform(rng, q, n)
     a_h[1] = (1 << 64) - 1  # exact first-stage path
     ref_poly, _ = oracle.polymul(a_h, b_h, n, q, w)
+    ref_lift = oracle.elemgtadd(oracle.elemmod(ref_poly, 65537, q), q // 3, 5)
     ref_fwd, _ = oracle.forward(a_h, n, q, w)
     saved = [L.vkhel_tune_get(f, log_n) for f in range(3)]
     try:
@@ -34,6 +35,8 @@ def test_every_variant_matches_oracle(vk, ctx, oracle, log_n):
             a, b, c = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h), vk.Vector(ctx, n)
             vk.polymul(a, b, c, t)
             np.testing.assert_array_equal(c.download(), ref_poly, err_msg=f"polymul variant {v}")
+            vk.polymul_lift(a, b, c, t, [("elemmod", 65537, 0), ("elemgtadd", q // 3, 5)])
+            np.testing.assert_array_equal(c.download(), ref_lift, err_msg=f"lifted polymul variant {v}")
             vk.forward_transform(a, c, t)
             np.testing.assert_array_equal(c.download(), ref_fwd, err_msg=f"forward variant {v}")
             vk.inverse_transform(c, c, t)

@@ -247,7 +247,7 @@ extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int nj
   if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
   if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
   if (log_n <= (uint32_t)kMaxCta) {
-    if (has_lift(lift)) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
+    if (has_lift(lift)) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n), *lift);
     return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
   }
   return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, has_lift(lift) ? lift : nullptr);

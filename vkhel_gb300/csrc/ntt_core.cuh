@@ -575,11 +575,12 @@ int inv_cta(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt
             int sms, int variant);
 int poly_cta(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
              int variant);
-// With an epilogue: default shape of each degree, one CTA per transform.
+// With an epilogue, one CTA per transform: the inverse in the default shape
+// of each degree, the polymul in the variant given.
 int inv_cta_lift(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n, int sms,
                  const vkcu_lift& lift);
 int poly_cta_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
-                  const vkcu_lift& lift);
+                  int variant, const vkcu_lift& lift);
 // cluster of 2^logc CTAs, n = 2^(14 + logc)
 int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
 int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,

@@ -1,6 +1,6 @@
 // Launcher of the CTA-resident fused polynomial multiplies with a fused
 // epilogue (the reference's centred-lift element-wise ops after the inverse
-// transform) for 2^8 <= n <= 2^14, default shape of each degree.
+// transform) for 2^8 <= n <= 2^14, every shape variant of each degree.
 #include "ntt_core.cuh"
 
 namespace vk {
@@ -19,9 +19,10 @@ static int launch_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, co
 }
 
 int poly_cta_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
-                  const vkcu_lift& lift) {
+                  int variant, const vkcu_lift& lift) {
+retry:
 #define X(L, E, U) launch_lift<L, E, U>(st, jobs, njobs, one, sms, lift)
-  VK_FOR_LOGN_DEFAULT(X)
+  VK_FOR_LOGN(X)
 #undef X
 }
 
