@@ -15,8 +15,9 @@ Reported on one JSON line (rank 0):
              alternate between two streams so consecutive batches overlap);
   e2e        the same through the public C API with host buffers: per step a
              pinned host -> device upload of a and b, the batch, and a
-             device -> host download of c, all inside the timed region, two
-             contexts pipelined;
+             device -> host download of c, all inside the timed region, steps
+             rotating over four contexts (streams) so copies and compute of
+             different steps overlap;
   roofline   the HBM roofline of the fused kernel (24 n bytes per limb product
              against the measured copy bandwidth) -- contract form;
   roofline_int  the binding roofline: Shoup modular multiplies per second
@@ -47,6 +48,7 @@ METRIC = "bit-exact polymul/s batched+served vs plain per-call on GB300; p50/p99
 UNIT = "limb-polymul/s"
 N, LIMBS, PAIRS, SEED = 16384, 8, 32, 2
 ROTATE = 4
+E2E_CTX = 4  # contexts (streams) the end-to-end steps rotate over
 WORKLOAD = (f"rns_batch: n={N}, {LIMBS} limbs (60-bit primes = 1 mod 2n), {PAIRS} pairs "
             f"= {PAIRS * LIMBS} limb-polymuls per step, seed {SEED}")
 
@@ -603,37 +605,48 @@ def main():
                     "imad_peak_per_s": imad_peak}
 
     # ---- end to end through the public API with pinned host buffers ----
-    # per step: upload a and b, run the batch, download c; steps alternate
-    # between the two contexts so one step's copies overlap the other's compute
+    # per step: upload a and b, run the batch, download c, all on one
+    # context's stream; steps rotate over E2E_CTX contexts so one step's
+    # uploads overlap other steps' compute and downloads (one stream per
+    # context: with two, a stream's upload -> compute -> download chain, not
+    # the host link, would bound the rate)
     L = vk.lib()
-    pins = []
-    for c in range(2):
+    e2e_ctxs = [vk.Context() for _ in range(E2E_CTX)]
+    e2e_sets, pins = [], []
+    for c in e2e_ctxs:
+        tb = [vk.NttTables(N, q, w) for q, w in zip(qs, ws)]
+        va, vb, vc = vk.Vector(c, words), vk.Vector(c, words), vk.Vector(c, words)
+        bt = vk.Batch(c)
+        for i in range(PAIRS):
+            bt.add_polymul(tb, va.device_ptr + 8 * i * stride, vb.device_ptr + 8 * i * stride,
+                           vc.device_ptr + 8 * i * stride)
+        bt.commit(graph=True)
+        e2e_sets.append((c, va, vb, vc, bt, tb))
         pa = torch.from_numpy(a_h.ravel().view(np.int64)).pin_memory()
         pb = torch.from_numpy(b_h.ravel().view(np.int64)).pin_memory()
         pc = torch.empty(words, dtype=torch.int64).pin_memory()
         pins.append((pa, pb, pc))
-    e2e_sets = [sets[0], sets[1]]
 
     def e2e_step(k):
-        c, va, vb, vc, bt = e2e_sets[k % 2]
-        pa, pb, pc = pins[k % 2]
+        c, va, vb, vc, bt, _ = e2e_sets[k % E2E_CTX]
+        pa, pb, pc = pins[k % E2E_CTX]
         L.vkhel_vector_upload_async(va.ptr, pa.data_ptr(), words)
         L.vkhel_vector_upload_async(vb.ptr, pb.data_ptr(), words)
         bt.launch()
         L.vkhel_vector_download_async(vc.ptr, pc.data_ptr(), words)
 
-    for k in range(4):
+    for k in range(2 * E2E_CTX):
         e2e_step(k)
-    for c in ctxs:
+    for c in e2e_ctxs:
         c.sync()
-    e2e_steps = max(4, min(args.steps, 400))
+    e2e_steps = max(2 * E2E_CTX, min(args.steps, 400))
     t0 = time.perf_counter()
     for k in range(e2e_steps):
         e2e_step(k)
-    for c in ctxs:
+    for c in e2e_ctxs:
         c.sync()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    for k in range(2):
+    for k in range(E2E_CTX):
         out = pins[k][2].numpy().view(np.uint64)
         for l in range(LIMBS):
             ref, _ = orc.polymul(a_h[0, l], b_h[0, l], N, qs[l], ws[l])
@@ -650,6 +663,7 @@ def main():
             c.sync()
         return (time.perf_counter() - t) / reps
     va0, vc1 = e2e_sets[0][1], e2e_sets[1][3]
+    ctxs = ctxs + e2e_ctxs  # copy_rate syncs every context
     h2d_s = copy_rate(lambda: L.vkhel_vector_upload_async(va0.ptr, pins[0][0].data_ptr(), words))
     d2h_s = copy_rate(lambda: L.vkhel_vector_download_async(vc1.ptr, pins[1][2].data_ptr(), words))
     both_s = copy_rate(lambda: (L.vkhel_vector_upload_async(va0.ptr, pins[0][0].data_ptr(), words),
@@ -660,7 +674,7 @@ def main():
            "copy_gbps": copy_gbps,
            "d2h_bytes_per_step": 8 * words, "ms_per_step": e2e_s * 1e3,
            "path": "vkhel_vector_upload_async x2 + vkhel_batch_launch + vkhel_vector_download_async, "
-                   "pinned host buffers, two contexts pipelined, host wall clock"}
+                   f"pinned host buffers, steps rotating over {E2E_CTX} contexts, host wall clock"}
 
     # ---- plain per-call path: the reference's call pattern on the GPU ----
     ctx0 = ctxs[0]
