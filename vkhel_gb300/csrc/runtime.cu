@@ -58,6 +58,14 @@ extern "C" int vkcu_pool_create(int device, void** pool) {
 
 extern "C" int vkcu_pool_destroy(void* pool) { return (int)cudaMemPoolDestroy((cudaMemPool_t)pool); }
 
+// Memory freed on one stream is reused by an allocation on another stream
+// only once the free has completed: the pool then never makes the allocating
+// stream wait for the freeing one (it grows instead).
+extern "C" int vkcu_pool_independent_streams(void* pool) {
+  int no = 0;
+  return (int)cudaMemPoolSetAttribute((cudaMemPool_t)pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+}
+
 extern "C" int vkcu_alloc(void* pool, void* stream, size_t bytes, void** ptr) {
   *ptr = nullptr;
   return (int)cudaMallocFromPoolAsync(ptr, bytes ? bytes : 8, (cudaMemPool_t)pool, (cudaStream_t)stream);

@@ -315,6 +315,11 @@ struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg) 
 	s->nslots = cfg && cfg->max_inflight_batches ? cfg->max_inflight_batches : 3;
 	s->slots = calloc(s->nslots, sizeof(*s->slots));
 	int e = !s->slots;
+	/* request buffers are allocated on the input stream and freed on the
+	 * output stream: without this the pool may make an upload wait for an
+	 * earlier micro-batch's download, serializing the two copy directions */
+	if (!e)
+		e = vkcu_pool_independent_streams(s->ctx->pool);
 	if (!e)
 		e = vkcu_stream_create(&s->s_in);
 	if (!e)
