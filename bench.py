@@ -158,9 +158,38 @@ def cpu_baseline_sample(qs, ws, a, b, budget_s=10.0):
         dt = time.perf_counter() - t0
         if dt > budget_s or done >= 8 * aa.shape[0]:
             break
+    # the same on one thread, on the first 64 limb products
+    one, t1 = 0, time.perf_counter()
+    while True:
+        orc.polymul_batch(aa[:64], bb[:64], N, qs, ws, pidx[:64], threads=1)
+        one += 64
+        dt1 = time.perf_counter() - t1
+        if dt1 > budget_s / 4:
+            break
     return {"value": done / dt, "unit": UNIT, "cores": used, "kind": "port",
             "sample": f"{done} limb-polymuls (the {aa.shape[0]}-limb batch x {done // aa.shape[0]}), n={N}, "
-                      f"{dt:.1f} s, oracle/oracle.c -O3, OpenMP over limbs"}
+                      f"{dt:.1f} s, oracle/oracle.c -O3, OpenMP over limbs",
+            "value_1_thread": one / dt1, "sample_1_thread": f"{one} limb-polymuls on one thread, {dt1:.1f} s",
+            "cpu_model": cpu_model(), "nproc": os.cpu_count()}
+
+
+def cpu_model():
+    """Host CPU model string (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def serving_sweep(vk, torch, rates=(1000, 4000, 16000, None), seconds=1.0, payloads=32, seed=4):
@@ -615,6 +644,9 @@ def main():
                     "frac": int_ach / (bfly_peak / 1e9),
                     "achieved_overlapped": int_ach_eff, "frac_overlapped": int_ach_eff / (bfly_peak / 1e9),
                     "modmuls_per_launch": modmuls,
+                    "imad_per_launch_model": 10 * modmuls,
+                    "imad_model": "about 10 32-bit IMAD-class multiplies per Shoup modmul (hi 64x64 = 4, two lo "
+                                  "64x64 = 3 each); the denominator is measured, not modelled",
                     "peak_source": "measured live: register-resident lazy CT butterflies (vkhel_measure_int_peak)",
                     "imad_peak_per_s": imad_peak}
 
@@ -728,6 +760,7 @@ def main():
         "clocks": clk,
         "kernel_ms_isolated_mean": kernel_ms,
         "kernel_ms_isolated_p50": statistics.median(iso_ms),
+        "kernel_ms_isolated_best": min(iso_ms),
         "plain": {"value": plain_rate, "unit": UNIT, "calls_per_limb_polymul": 4,
                   "latency_ms_p50": pct(lat_ms, 0.5), "latency_ms_p99": pct(lat_ms, 0.99)},
         "speedup_vs_plain": value / plain_rate,
