@@ -53,6 +53,11 @@ uint64_t vkhel_launch_count(void);
  * second.  Allocates and frees a few KB of device memory. */
 int vkhel_measure_int_peak(struct vkhel_ctx *ctx, double *butterflies_per_s,
 		double *imad_per_s);
+/* Fault injection for tests (host side, process-wide): after `skip` more
+ * device allocations by this library, the next `count` fail with
+ * VKHEL_ERR_OUT_OF_MEMORY as if the device had run out of memory.
+ * count = 0 switches it off. */
+int vkhel_debug_fail_allocations(uint64_t skip, uint64_t count);
 
 /* ---- vectors ---- */
 uint64_t vkhel_vector_length(const struct vkhel_vector *v);
@@ -259,6 +264,10 @@ struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg);
 int64_t vkhel_server_submit(struct vkhel_server *s,
 		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *b, uint64_t *c);
+/* Cancels request `id` if it is still queued (not yet in a micro-batch): its
+ * wait then returns VKHEL_ERR_CANCELLED.  Fails with INVALID_ARGUMENT for a
+ * request that is running, finished, collected or unknown. */
+int vkhel_server_cancel(struct vkhel_server *s, int64_t id);
 /* Waits up to timeout_ms for request `id`; returns its status, or
  * VKHEL_ERR_TIMEOUT (the request stays pending and can be waited for again).
  * After a non-timeout return the id is collected and cannot be waited again. */

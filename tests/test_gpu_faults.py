@@ -1,0 +1,138 @@
+"""Failure paths, injected on the host.
+
+Device allocations are made to fail by the library's host-side injector
+(vkhel_debug_fail_allocations) -- no GPU fault is involved.  Every entry point
+must report the failure as a status (or a NULL object), leave the context
+usable, and give correct results once allocations succeed again; a server
+fails only the micro-batch whose allocation failed.  Queued server requests
+can be cancelled.
+"""
+import numpy as np
+import pytest
+
+from vkhel_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+OOM, BUDGET, CANCELLED = 2, 3, 7
+
+
+@pytest.fixture(autouse=True)
+def _injector_off(vk):
+    yield
+    vk.fail_allocations(0, 0)
+
+
+def _operands(n, seed=0):
+    q = workloads.ntt_primes(n, 1)[0]
+    w = workloads.root_for(n, q)
+    rng = np.random.default_rng(seed)
+    return q, w, workloads.uniform(rng, q, n), workloads.uniform(rng, q, n)
+
+
+def test_vector_creation_failure_is_reported_and_recovers(vk, ctx):
+    before = ctx.bytes_in_use
+    vk.fail_allocations(0, 1)
+    with pytest.raises(vk.VkhelError) as e:
+        vk.Vector(ctx, 1024)
+    assert e.value.code == OOM
+    assert ctx.bytes_in_use == before
+    v = vk.Vector(ctx, np.arange(1024, dtype=np.uint64))
+    np.testing.assert_array_equal(v.download(), np.arange(1024, dtype=np.uint64))
+
+
+def test_polymul_scratch_failure_then_success(vk, ctx, oracle):
+    n = 1 << 12
+    q, w, a_h, b_h = _operands(n)
+    t = vk.NttTables(n, q, w)
+    a, b, c = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h), vk.Vector(ctx, n)
+    vk.polymul(a, b, c, t)              # tables resident; no scratch needed for a separate result
+    vk.fail_allocations(0, 1)           # result aliases a: the call needs a scratch buffer
+    with pytest.raises(vk.VkhelError) as e:
+        vk.polymul(a, b, a, t)
+    assert e.value.code == OOM
+    np.testing.assert_array_equal(a.download(), a_h)   # nothing ran
+    vk.polymul(a, b, a, t)
+    np.testing.assert_array_equal(a.download(), oracle.polymul(a_h, b_h, n, q, w)[0])
+
+
+def test_batch_commit_failure_then_fresh_batch(vk, ctx, oracle):
+    n = 1 << 14
+    q, w, a_h, b_h = _operands(n, 1)
+    t = vk.NttTables(n, q, w)
+    a, b, c = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h), vk.Vector(ctx, n)
+    bt = vk.Batch(ctx)
+    bt.add_polymul([t], a, b, c)
+    vk.fail_allocations(0, 1)           # the device job table
+    with pytest.raises(vk.VkhelError) as e:
+        bt.commit()
+    assert e.value.code == OOM
+    bt.close()
+    bt = vk.Batch(ctx)
+    bt.add_polymul([t], a, b, c)
+    bt.commit()
+    bt.run()
+    np.testing.assert_array_equal(c.download(), oracle.polymul(a_h, b_h, n, q, w)[0])
+
+
+def test_table_upload_failure_then_success(vk, ctx, oracle):
+    n = 1 << 10
+    q, w, a_h, _ = _operands(n, 2)
+    t = vk.NttTables(n, q, w)
+    a, r = vk.Vector(ctx, a_h), vk.Vector(ctx, n)
+    vk.fail_allocations(0, 1)           # the context's first use of (n, q, w): its device tables
+    with pytest.raises(vk.VkhelError):
+        vk.forward_transform(a, r, t)
+    vk.forward_transform(a, r, t)
+    np.testing.assert_array_equal(r.download(), oracle.forward(a_h, n, q, w)[0])
+
+
+def test_budget_exhaustion(vk, ctx):
+    ctx.set_budget(ctx.bytes_in_use + 8 * 1024)
+    try:
+        vk.Vector(ctx, 512)
+        with pytest.raises(vk.VkhelError) as e:
+            vk.Vector(ctx, 4096)
+        assert e.value.code == BUDGET
+    finally:
+        ctx.set_budget(0)
+
+
+def test_server_fails_only_the_failing_micro_batch(vk, oracle):
+    n = 1 << 13
+    q, w, a_h, b_h = _operands(n, 3)
+    t = vk.NttTables(n, q, w)
+    ref = oracle.polymul(a_h, b_h, n, q, w)[0]
+    with vk.Server(max_batch_limbs=4) as srv:
+        srv.wait(srv.submit([t], a_h, b_h, np.zeros(n, np.uint64)))   # warm-up: tables resident
+        c1 = np.zeros(n, np.uint64)
+        vk.fail_allocations(0, 1)
+        assert srv.wait(srv.submit([t], a_h, b_h, c1)) == OOM
+        c2 = np.zeros(n, np.uint64)
+        assert srv.wait(srv.submit([t], a_h, b_h, c2)) == 0
+        np.testing.assert_array_equal(c2, ref)
+        assert srv.stats()["failed"] >= 1
+
+
+def test_server_cancel_queued_request(vk, oracle):
+    n = 1 << 16
+    q, w, a_h, b_h = _operands(n, 4)
+    t = vk.NttTables(n, q, w)
+    limbs = 8
+    a = np.tile(a_h, limbs)
+    b = np.tile(b_h, limbs)
+    per = 3 * limbs * n * 8
+    # one request at a time (budget), many queued: the last is still queued when cancelled
+    with vk.Server(device_budget=per, max_batch_limbs=limbs, max_inflight_batches=1) as srv:
+        outs = [np.zeros(limbs * n, np.uint64) for _ in range(12)]
+        ids = [srv.submit([t] * limbs, a, b, o) for o in outs]
+        st = srv.cancel(ids[-1])
+        results = [srv.wait(i) for i in ids]
+        assert all(r == 0 for r in results[:-1])
+        if st == 0:
+            assert results[-1] == CANCELLED
+        else:  # it had already started: it must then have completed normally
+            assert results[-1] == 0
+        assert srv.cancel(ids[0]) != 0      # collected: cannot be cancelled
+    ref = oracle.polymul(a_h, b_h, n, q, w)[0]
+    np.testing.assert_array_equal(outs[0][:n], ref)

@@ -79,6 +79,8 @@ _SIGNATURES = [
     ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_lift", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp, vp, u32]),
+    ("vkhel_debug_fail_allocations", ctypes.c_int, [u64, u64]),
+    ("vkhel_server_cancel", ctypes.c_int, [vp, ctypes.c_int64]),
     ("vkhel_elem_batch_create", vp, [vp]),
     ("vkhel_elem_batch_add", ctypes.c_int, [vp, u32, u64, u64, u64, vp, vp, vp]),
     ("vkhel_elem_batch_add_raw", ctypes.c_int, [vp, u32, u64, u64, u64, vp, vp, vp, u64]),
@@ -411,6 +413,11 @@ def launch_count():
     return lib().vkhel_launch_count()
 
 
+def fail_allocations(skip, count):
+    """Test fault injection: after `skip` device allocations the next `count` fail."""
+    lib().vkhel_debug_fail_allocations(int(skip), int(count))
+
+
 class Batch:
     """vkhel_batch: a committed list of limb products launched as one unit."""
 
@@ -559,6 +566,13 @@ class Server:
             raise VkhelError(-rid, msg)
         self._pending[rid] = (tables, a, b, c)
         return rid
+
+    def cancel(self, rid):
+        """Cancel a request still queued; returns its status code (0 = cancelled)."""
+        st = lib().vkhel_server_cancel(self.ptr, rid)
+        if st:
+            lib().vkhel_ctx_clear_error(None)
+        return st
 
     def wait(self, rid, timeout_ms=60000):
         st = lib().vkhel_server_wait(self.ptr, rid, int(timeout_ms))

@@ -9,6 +9,7 @@
  * fence after every submit.
  */
 #include <inttypes.h>
+#include <stdatomic.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -50,7 +51,37 @@ int vkh_cuda(struct vkhel_ctx *ctx, int err, const char *what) {
 	return vkh_fail(ctx, code, "%s: CUDA error %d (%s)", what, err, vkcu_error_string(err));
 }
 
+/* Host-side fault injection for tests: after `skip` more device allocations,
+ * the next `count` fail as if the device were out of memory. */
+static _Atomic uint64_t g_fail_skip, g_fail_count;
+
+int vkhel_debug_fail_allocations(uint64_t skip, uint64_t count) {
+	g_fail_count = 0;
+	g_fail_skip = skip;
+	g_fail_count = count;
+	return VKHEL_OK;
+}
+
+int vkh_inject_alloc_failure(void) {
+	for (;;) {
+		uint64_t c = g_fail_count;
+		if (c == 0)
+			return 0;
+		uint64_t k = g_fail_skip;
+		if (k > 0) {
+			if (atomic_compare_exchange_weak(&g_fail_skip, &k, k - 1))
+				return 0;
+			continue;
+		}
+		if (atomic_compare_exchange_weak(&g_fail_count, &c, c - 1))
+			return 1;
+	}
+}
+
 int vkh_dev_alloc(struct vkhel_ctx *ctx, uint64_t bytes, void **ptr) {
+	if (vkh_inject_alloc_failure())
+		return vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "device allocation of %" PRIu64 " bytes failed (injected)",
+				bytes);
 	if (ctx->budget && ctx->in_use + bytes > ctx->budget)
 		return vkh_fail(ctx, VKHEL_ERR_BUDGET,
 				"device budget: %" PRIu64 " + %" PRIu64 " bytes exceeds %" PRIu64,

@@ -86,6 +86,8 @@ void vkh_dev_free(struct vkhel_ctx *ctx, void *ptr, uint64_t bytes);
 int vkh_devtab_get(struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t,
 		const struct vkh_devtab **out);
 void vkh_devtab_release_all(struct vkhel_ctx *ctx);
+/* api.c -- 1 when the test fault injector fails this device allocation */
+int vkh_inject_alloc_failure(void);
 /* api.c -- modulus check of the element-wise ops (mod >= 2) */
 int vkh_check_mod(struct vkhel_ctx *ctx, const char *op, uint64_t mod);
 /* api.c -- centred-lift steps to the device form; q = 0 leaves ELEMMOD's

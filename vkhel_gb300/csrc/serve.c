@@ -111,7 +111,8 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 		struct srv_req *r = sl->reqs[i];
 		const uint64_t words = (uint64_t) r->limbs * r->n;
 		const int fused = fused_log_n(r->log_n);
-		int e = vkcu_alloc(ctx->pool, s->s_in, r->dev_bytes, &r->dev);
+		int e = vkh_inject_alloc_failure() ? VKHEL_ERR_OUT_OF_MEMORY
+		                                   : vkcu_alloc(ctx->pool, s->s_in, r->dev_bytes, &r->dev);
 		if (!e)
 			e = vkcu_h2d(s->s_in, r->dev, r->a, 8 * words);
 		if (!e)
@@ -467,6 +468,41 @@ int vkhel_server_wait(struct vkhel_server *s, int64_t id, uint32_t timeout_ms) {
 	free(r->tables);
 	free(r);
 	return st;
+}
+
+int vkhel_server_cancel(struct vkhel_server *s, int64_t id) {
+	if (!s || id < 1)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_cancel: bad arguments");
+	pthread_mutex_lock(&s->mu);
+	if (id >= s->next_id || !s->by_id[id - 1]) {
+		pthread_mutex_unlock(&s->mu);
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_cancel: unknown or already collected id %lld",
+				(long long) id);
+	}
+	struct srv_req *r = s->by_id[id - 1];
+	if (r->state != 0) {
+		pthread_mutex_unlock(&s->mu);
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_cancel: request %lld is already %s",
+				(long long) id, r->state == 1 ? "running" : "finished");
+	}
+	/* unlink from the queue */
+	struct srv_req *prev = NULL;
+	for (struct srv_req *q = s->q_head; q && q != r; q = q->next)
+		prev = q;
+	if (prev)
+		prev->next = r->next;
+	else
+		s->q_head = r->next;
+	if (s->q_tail == r)
+		s->q_tail = prev;
+	r->next = NULL;
+	r->state = 2;
+	r->status = VKHEL_ERR_CANCELLED;
+	r->t_done = now_s();
+	s->failed++;
+	pthread_cond_broadcast(&s->cv_done);
+	pthread_mutex_unlock(&s->mu);
+	return VKHEL_OK;
 }
 
 static int cmp_double(const void *x, const void *y) {
