@@ -484,8 +484,7 @@ static int check_transform(const char *op, const struct vkhel_vector *a, const s
 	return vkh_devtab_get(res->ctx, t, d);
 }
 
-void vkhel_vector_forward_transform(const struct vkhel_vector *a, struct vkhel_vector *res,
-		struct vkhel_ntt_tables *t) {
+static void forward_impl(const struct vkhel_vector *a, struct vkhel_vector *res, struct vkhel_ntt_tables *t) {
 	const struct vkh_devtab *d = NULL;
 	if (check_transform("forward_transform", a, res, t, &d))
 		return;
@@ -494,6 +493,13 @@ void vkhel_vector_forward_transform(const struct vkhel_vector *a, struct vkhel_v
 	const vkcu_ntt_job job = {a->dev, res->dev, d->dev_set};
 	finish(res->ctx, vkcu_ntt_forward(res->ctx->stream, NULL, 1, &job, t->log_n, res->ctx->sms),
 			"forward_transform");
+}
+
+void vkhel_vector_forward_transform(const struct vkhel_vector *a, struct vkhel_vector *res,
+		struct vkhel_ntt_tables *t) {
+	vkcu_range_push("vkhel_vector_forward_transform");
+	forward_impl(a, res, t);
+	vkcu_range_pop();
 }
 
 static int inverse_impl(const struct vkhel_vector *a, struct vkhel_vector *res, struct vkhel_ntt_tables *t,
@@ -525,12 +531,17 @@ static int inverse_impl(const struct vkhel_vector *a, struct vkhel_vector *res, 
 
 void vkhel_vector_inverse_transform(const struct vkhel_vector *a, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t) {
+	vkcu_range_push("vkhel_vector_inverse_transform");
 	inverse_impl(a, res, t, NULL, 0);
+	vkcu_range_pop();
 }
 
 int vkhel_vector_inverse_transform_lift(const struct vkhel_vector *a, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
-	return inverse_impl(a, res, t, steps, nsteps);
+	vkcu_range_push("vkhel_vector_inverse_transform_lift");
+	const int st = inverse_impl(a, res, t, steps, nsteps);
+	vkcu_range_pop();
+	return st;
 }
 
 /* The reference's element-wise ops as epilogue steps, with the constants its
@@ -596,12 +607,18 @@ static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector 
 
 int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t) {
-	return polymul_impl(a, b, res, t, NULL, 0);
+	vkcu_range_push("vkhel_vector_polymul");
+	const int st = polymul_impl(a, b, res, t, NULL, 0);
+	vkcu_range_pop();
+	return st;
 }
 
 int vkhel_vector_polymul_lift(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
-	return polymul_impl(a, b, res, t, steps, nsteps);
+	vkcu_range_push("vkhel_vector_polymul_lift");
+	const int st = polymul_impl(a, b, res, t, steps, nsteps);
+	vkcu_range_pop();
+	return st;
 }
 
 static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,

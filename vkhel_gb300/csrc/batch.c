@@ -386,6 +386,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 int vkhel_batch_launch(struct vkhel_batch *b) {
 	if (!b || !b->committed)
 		return vkh_fail(b ? b->ctx : NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_launch: not committed");
+	vkcu_range_push("vkhel_batch_launch");
 	int e;
 	if (b->graph) {
 		e = vkcu_graph_launch(b->graph, b->ctx->stream);
@@ -394,6 +395,7 @@ int vkhel_batch_launch(struct vkhel_batch *b) {
 	} else {
 		e = issue(b);
 	}
+	vkcu_range_pop();
 	return vkh_cuda(b->ctx, e, "batch_launch");
 }
 

@@ -279,6 +279,7 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 int vkhel_elem_batch_launch(struct vkhel_elem_batch *b) {
 	if (!b || !b->committed)
 		return vkh_fail(b ? b->ctx : NULL, VKHEL_ERR_INVALID_ARGUMENT, "elem_batch_launch: not committed");
+	vkcu_range_push("vkhel_elem_batch_launch");
 	int e = 0;
 	if (b->graph) {
 		e = vkcu_graph_launch(b->graph, b->ctx->stream);
@@ -287,6 +288,7 @@ int vkhel_elem_batch_launch(struct vkhel_elem_batch *b) {
 	} else if (b->chunks) {
 		e = vkcu_elem_batch(b->ctx->stream, b->dev, b->chunks, b->ctx->sms);
 	}
+	vkcu_range_pop();
 	return vkh_cuda(b->ctx, e, "elem_batch_launch");
 }
 

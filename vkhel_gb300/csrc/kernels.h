@@ -53,6 +53,9 @@ int vkcu_stream_destroy(void *stream);
 int vkcu_pool_create(int device, void **pool);
 int vkcu_pool_destroy(void *pool);
 int vkcu_pool_independent_streams(void *pool);
+/* Profiler ranges (NVTX) around entry points. */
+void vkcu_range_push(const char *name);
+void vkcu_range_pop(void);
 int vkcu_alloc(void *pool, void *stream, size_t bytes, void **ptr);
 int vkcu_free(void *stream, void *ptr);
 int vkcu_memset0(void *stream, void *ptr, size_t bytes);

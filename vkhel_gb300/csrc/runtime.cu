@@ -9,6 +9,7 @@
 //    driver (the role VMA plays in the reference);
 //  * plain stream-ordered copies; pinned host memory for mapped windows.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdint>
@@ -55,6 +56,11 @@ extern "C" int vkcu_pool_create(int device, void** pool) {
   *pool = p;
   return (int)e;
 }
+
+// NVTX ranges around the library's entry points (header-only NVTX v3: no
+// cost unless a profiler is attached).
+extern "C" void vkcu_range_push(const char* name) { nvtxRangePushA(name); }
+extern "C" void vkcu_range_pop(void) { nvtxRangePop(); }
 
 extern "C" int vkcu_pool_destroy(void* pool) { return (int)cudaMemPoolDestroy((cudaMemPool_t)pool); }
 

@@ -102,6 +102,7 @@ static int cmp_job_log_n(const void *x, const void *y) {
 /* Enqueue one micro-batch on the server streams (called without the lock). */
 static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 	struct vkhel_ctx *ctx = s->ctx;
+	vkcu_range_push("vkhel_server micro-batch");
 	uint32_t njobs = 0;
 	/* keys: log_n in the high bits, running index in the low bits -> stable sort */
 	uint64_t *keys = malloc(sizeof(uint64_t) * (s->max_limbs + 64) * 2);
@@ -196,6 +197,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 	vkcu_event_record(sl->ev_done, s->s_out);
 	free(keys);
 	free(tmp);
+	vkcu_range_pop();
 }
 
 /* Mark a finished slot's requests done (lock held). */
