@@ -501,7 +501,47 @@ def device_twiddles(vk, ctx, torch, orc=None):
     return out
 
 
+def standalone_ops(vk, ctx, torch, orc, words=1 << 27, reps=5):
+    """Each public element-wise call on 2^27-word (1 GiB) vectors (61-bit
+    modulus, uniform operands, seed 7): device time per call (CUDA events on
+    the context stream; the call's own synchronisation is inside the
+    bracket) and GB/s of its algorithmic bytes against the HBM copy peak; and
+    single-call forward / inverse transforms (n = 2^14 and 2^17) with their
+    latency.  Spot-checked against the oracle."""
+    from vkhel_gb300 import workloads
+    rng = np.random.default_rng(7)
+    q = (1 << 61) - 1
+    a = vk.Vector(ctx, workloads.uniform(rng, q, words))
+    b = vk.Vector(ctx, workloads.uniform(rng, q, words))
+    r = vk.Vector(ctx, words)
+    peak = load_peaks()[0].get("hbm_gbs", 6800.0)
+    ops = {"elemmul": (lambda: vk.elemmul(a, b, r, q), 24), "elemfma": (lambda: vk.elemfma(a, b, r, 12345, q), 24),
+           "elemgtadd": (lambda: vk.elemgtadd(a, r, q // 2, 17), 16),
+           "elemgtsub": (lambda: vk.elemgtsub(a, r, q // 2, q, 65537), 16),
+           "elemmod": (lambda: vk.elemmod(a, r, 65537, q), 16)}
+    out = {"workload": f"{words} words per vector, 61-bit modulus, seed 7", "hbm_peak_gbs": peak, "ops": {}}
+    for name, (fn, bpw) in ops.items():
+        sec = _event_time(torch, ctx, fn, reps)
+        out["ops"][name] = {"ms": sec * 1e3, "gbs": bpw * words / sec / 1e9, "hbm_frac": bpw * words / sec / 1e9 / peak}
+    k = 1 << 16
+    got = r.download(k)
+    ref = orc.elemmod(a.download(k), 65537, q)
+    assert np.array_equal(got, ref), "standalone elemmod differs from the oracle"
+    for log_n in (14, 17):
+        n = 1 << log_n
+        qq = workloads.ntt_primes(n, 1)[0]
+        t = vk.NttTables(n, qq, workloads.root_for(n, qq))
+        x = vk.Vector(ctx, workloads.uniform(rng, qq, n))
+        y = vk.Vector(ctx, n)
+        fwd = _event_time(torch, ctx, lambda: vk.forward_transform(x, y, t), 50)
+        inv = _event_time(torch, ctx, lambda: vk.inverse_transform(y, y, t), 50)
+        out[f"forward_n{n}_us"] = fwd * 1e6
+        out[f"inverse_n{n}_us"] = inv * 1e6
+    return out
+
+
 EXTRAS = {"single_limb_batch": single_limb_batch, "ragged_batch": ragged_batch,
+          "standalone_ops": standalone_ops,
           "lift_epilogue": lift_epilogue, "elementwise_batch": elementwise_batch,
           "device_twiddles": device_twiddles}
 
