@@ -142,7 +142,9 @@ static int simple(cudaStream_t st, bool inverse, const vkcu_ntt_job* jobs, int n
   const int threads = n / 2 < 32 ? 32 : (n / 2 > 512 ? 512 : n / 2);
   const int smem = n * 8;
   auto kern = inverse ? k_ntt_inv_simple : k_ntt_fwd_simple;
-  if (int e = prepare(kern, smem)) return e;
+  // opted in once per device for the largest n this path takes (2^14)
+  static std::atomic<unsigned> prepared_fwd{0}, prepared_inv{0};
+  if (int e = prepare(kern, (1 << kMaxCta) * 8, inverse ? prepared_inv : prepared_fwd)) return e;
   const int grid = grid_for(kern, threads, smem, njobs, sms);
   kern<<<grid, threads, smem, st>>>(jobs, njobs, one, log_n);
   vkcu_count_launches(1);

@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(512, 1)
 template <int LOGC, auto kern, class... Args>
 static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   constexpr int C = 1 << LOGC;
-  static const int prepared = prepare(kern, SubShape::SMEM_BYTES);
-  if (prepared) return prepared;
+  static std::atomic<unsigned> prepared{0};
+  if (const int e = prepare(kern, SubShape::SMEM_BYTES, prepared)) return e;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;

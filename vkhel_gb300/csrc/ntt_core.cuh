@@ -37,6 +37,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <type_traits>
 
 #include "arith.cuh"
@@ -588,9 +589,18 @@ int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu
 int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
                  const vkcu_lift* lift = nullptr);
 
+// Opts `kernel` into `smem` bytes of dynamic shared memory.  The attribute
+// is per device, so it is set once per device (bit d of `done`; devices
+// beyond 31 set it on every call).
 template <class K>
-static int prepare(K kernel, int smem) {
-  return (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+static int prepare(K kernel, int smem, std::atomic<unsigned>& done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  const unsigned bit = dev >= 0 && dev < 32 ? 1u << dev : 0u;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return 0;
+  const int e = (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (!e && bit) done.fetch_or(bit, std::memory_order_release);
+  return e;
 }
 
 template <class K>

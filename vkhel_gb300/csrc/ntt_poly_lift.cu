@@ -10,8 +10,8 @@ static int launch_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, co
                        const vkcu_lift& lift) {
   using S = Shape<LOGN, E, U>;
   auto kern = k_polymul<LOGN, E, U, true>;
-  static const int prepared = prepare(kern, S::SMEM_BYTES);
-  if (prepared) return prepared;
+  static std::atomic<unsigned> prepared{0};
+  if (const int e = prepare(kern, S::SMEM_BYTES, prepared)) return e;
   const int grid = grid_for(kern, S::T, S::SMEM_BYTES, (long)njobs, sms);
   kern<<<grid, S::T, S::SMEM_BYTES, st>>>(jobs, njobs, one, lift);
   vkcu_count_launches(1);
