@@ -28,6 +28,8 @@ def test_every_variant_matches_oracle(vk, ctx, oracle, log_n):
     ref_lift = oracle.elemgtadd(oracle.elemmod(ref_poly, 65537, q), q // 3, 5)
     ref_fwd, _ = oracle.forward(a_h, n, q, w)
     saved = [L.vkhel_tune_get(f, log_n) for f in range(3)]
+    split = L.vkhel_tune_get(3, 1)
+    L.vkhel_tune_set(3, 1, 1)  # single calls on one CTA (not split over a cluster): the variants run
     try:
         for v in VARIANTS[log_n]:
             for f in range(3):
@@ -45,6 +47,39 @@ def test_every_variant_matches_oracle(vk, ctx, oracle, log_n):
     finally:
         for f in range(3):
             L.vkhel_tune_set(f, log_n, saved[f])
+        L.vkhel_tune_set(3, 1, split)
+
+
+@pytest.mark.parametrize("log_n", [13, 14])
+@pytest.mark.parametrize("split", [0, 1])
+def test_single_calls_split_or_not_are_exact(vk, ctx, oracle, log_n, split):
+    """A single call of n = 2^13 / 2^14 runs on an 8-CTA cluster (2^10 / 2^11-word
+    sub-blocks) unless the split is switched off; both give the oracle's words."""
+    L = vk.lib()
+    n = 1 << log_n
+    q = workloads.ntt_primes(n, 1, bound=1 << 62)[0]
+    w = workloads.root_for(n, q)
+    t = vk.NttTables(n, q, w)
+    rng = np.random.default_rng(log_n + 40 * split)
+    a_h, b_h = workloads.uniform(rng, q, n), workloads.uniform(rng, q, n)
+    a_h[3] = (1 << 64) - 1  # exact first-stage rule
+    saved = L.vkhel_tune_get(3, 1)
+    try:
+        L.vkhel_tune_set(3, 1, split)
+        a, b, c = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h), vk.Vector(ctx, n)
+        vk.polymul(a, b, c, t)
+        np.testing.assert_array_equal(c.download(), oracle.polymul(a_h, b_h, n, q, w)[0])
+        vk.polymul_lift(a, b, c, t, [("elemmod", 2, 0)])
+        np.testing.assert_array_equal(c.download(), oracle.elemmod(oracle.polymul(a_h, b_h, n, q, w)[0], 2, q))
+        vk.forward_transform(a, c, t)
+        np.testing.assert_array_equal(c.download(), oracle.forward(a_h, n, q, w)[0])
+        x = c.download()
+        x[5] = (1 << 64) - 3  # unreduced input to the inverse
+        c.upload(x)
+        vk.inverse_transform(c, c, t)
+        np.testing.assert_array_equal(c.download(), oracle.inverse(x, n, q, w)[0])
+    finally:
+        L.vkhel_tune_set(3, 1, saved)
 
 
 @pytest.mark.parametrize("concurrent", [0, 1])

@@ -192,6 +192,14 @@ static bool jobs_aligned(const vkcu_ntt_job* jobs, const vkcu_ntt_job* one) {
   return jobs != nullptr || (aligned32(one->in) && aligned32(one->out));
 }
 
+// Few jobs of n = 2^13 or 2^14 (at most one per 8 SMs, e.g. a single call):
+// each runs on a cluster of 8 CTAs with 2^10 / 2^11-word sub-blocks instead
+// of one CTA, so it uses 8 SMs.  Tuning entry (family 3, log_n 1) = 1 turns
+// this off.
+static bool split_small(int njobs, uint32_t log_n, int sms) {
+  return (log_n == 13 || log_n == 14) && (long)njobs * 8 <= (long)sms && vkh_variant(3, 1) == 0;
+}
+
 extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
                                 uint32_t log_n, int sms) {
   cudaStream_t st = (cudaStream_t)stream;
@@ -200,8 +208,9 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
   const bool aligned = jobs_aligned(jobs, one);
   if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, false, jobs, njobs, o, (int)log_n, sms);
   if (!aligned) return (int)cudaErrorMisalignedAddress;
+  if (split_small(njobs, log_n, sms)) return fwd_cluster(st, jobs, njobs, o, 3, (int)log_n - 3);
   if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(1, (int)log_n));
-  if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta);
+  if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta);
   const int kk = (int)log_n - kMaxCta;
   if (int e = global_pass<false>(st, jobs, njobs, o, (int)log_n, kk, sms)) return e;
   return fwd_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(1, kMaxCta));
@@ -222,11 +231,13 @@ extern "C" int vkcu_ntt_inverse_lift(void* stream, const vkcu_ntt_job* jobs, int
     e = simple(st, true, jobs, njobs, o, (int)log_n, sms);
   } else if (!aligned) {
     return (int)cudaErrorMisalignedAddress;
+  } else if (split_small(njobs, log_n, sms)) {
+    return inv_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lifted ? lift : nullptr);
   } else if (log_n <= (uint32_t)kMaxCta) {
     if (lifted) return inv_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
     return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(2, (int)log_n));
   } else if (log_n <= (uint32_t)kMaxCluster) {
-    return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, lifted ? lift : nullptr);
+    return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lifted ? lift : nullptr);
   } else {
     const int kk = (int)log_n - kMaxCta;
     e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(2, kMaxCta));
@@ -248,11 +259,12 @@ extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int nj
   const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
   if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
   if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
+  if (split_small(njobs, log_n, sms)) return poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, has_lift(lift) ? lift : nullptr);
   if (log_n <= (uint32_t)kMaxCta) {
     if (has_lift(lift)) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n), *lift);
     return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
   }
-  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, has_lift(lift) ? lift : nullptr);
+  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, has_lift(lift) ? lift : nullptr);
 }
 
 extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,

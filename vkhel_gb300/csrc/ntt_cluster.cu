@@ -17,6 +17,10 @@
 //             column from the C CTAs over DSMEM and runs the last log2 C
 //             stages with n^-1 folded in, writing global memory coalesced.
 //
+// The sub-block is 2^14 words (n = 2^15 .. 2^17, one CTA per SM), or 2^10 /
+// 2^11 words for n = 2^13 / 2^14 split over 8 CTAs when there are too few
+// jobs to fill the GPU with one CTA per job (single calls).
+//
 // Cluster barriers separate the phases: before a column pass writes another
 // CTA's shared memory (its owner has finished reading it), after it (the
 // sub-blocks are complete), and before the inverse gather.  Every CTA of a
@@ -30,23 +34,23 @@ namespace cg = cooperative_groups;
 
 namespace vk {
 
-using SubShape = Shape<14, 32>;
+using SubShape = Shape<14, 32>;  // the large-n sub-block
 
-template <int LOGC>
+template <int LOGC, class S>
 struct Cols {
-  static constexpr int C = 1 << LOGC, SUB = 1 << 14;
-  static constexpr int COLS = SUB >> LOGC;        // columns per CTA
-  static constexpr int PER = COLS / SubShape::T;  // columns per thread
-  static_assert(PER * C == SubShape::E, "a column pass moves E words per thread");
-  __device__ __forceinline__ static int col(int rank, int k) { return rank * COLS + (int)threadIdx.x + k * SubShape::T; }
+  static constexpr int C = 1 << LOGC, SUB = S::N;
+  static constexpr int COLS = SUB >> LOGC;  // columns per CTA
+  static constexpr int PER = COLS / S::T;   // columns per thread
+  static_assert(PER * C == S::E, "a column pass moves E words per thread");
+  __device__ __forceinline__ static int col(int rank, int k) { return rank * COLS + (int)threadIdx.x + k * S::T; }
 };
 
 // Forward column pass: global stages 0 .. LOGC-1 (exact first-stage rule),
 // outputs scattered to the owning CTAs' shared memory, lazy [0, 4q).
-template <int LOGC>
+template <int LOGC, class S>
 __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, const cg::cluster_group& cl, int rank,
                                         const Tw& t) {
-  using K = Cols<LOGC>;
+  using K = Cols<LOGC, S>;
   u64 v[K::PER * K::C];
 #pragma unroll
   for (int k = 0; k < K::PER; k++)
@@ -69,10 +73,10 @@ __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, con
 
 // Inverse column pass: gather, global stages LOGC-1 .. 0 with n^-1 folded in,
 // canonical words to global memory.
-template <int LOGC, class Epi>
+template <int LOGC, class S, class Epi>
 __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
                                         const Tw& t, const Epi& epi) {
-  using K = Cols<LOGC>;
+  using K = Cols<LOGC, S>;
   u64 v[K::PER * K::C];
 #pragma unroll
   for (int j = 0; j < K::C; j++) {
@@ -90,20 +94,19 @@ __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg
     for (int j = 0; j < K::C; j++) out[K::col(rank, k) + (size_t)j * K::SUB] = epi(v[k * K::C + j]);
 }
 
-template <int LOGC, bool LIFT>
+template <int LOGC, class S, bool LIFT>
 __device__ __forceinline__ void col_inv_out(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
                                             const Tw& t, const vkcu_lift* lift) {
   if constexpr (LIFT)
-    col_inv<LOGC>(out, sm, cl, rank, t, LiftRun(lift, t.q));
+    col_inv<LOGC, S>(out, sm, cl, rank, t, LiftRun(lift, t.q));
   else
-    col_inv<LOGC>(out, sm, cl, rank, t, NoLift{});
+    col_inv<LOGC, S>(out, sm, cl, rank, t, NoLift{});
 }
 
-template <int LOGC>
-__global__ void __launch_bounds__(512, 1)
+template <int LOGC, class S>
+__global__ void __launch_bounds__(S::T, 1)
     k_ntt_fwd_cluster(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one) {
-  using S = SubShape;
-  using K = Cols<LOGC>;
+  using K = Cols<LOGC, S>;
   extern __shared__ u64 sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(512, 1)
     const Tw t = load_tw(job.tw);
     u64* out = reinterpret_cast<u64*>(job.out) + (size_t)rank * K::SUB;
     cl.sync();
-    col_fwd<LOGC>(reinterpret_cast<const u64*>(job.in), sm, cl, rank, t);
+    col_fwd<LOGC, S>(reinterpret_cast<const u64*>(job.in), sm, cl, rank, t);
     cl.sync();
     fwd_first_smem<S>(sm, t, tw_mult);
     fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
@@ -127,12 +130,11 @@ __global__ void __launch_bounds__(512, 1)
   cl.sync();
 }
 
-template <int LOGC, bool LIFT>
-__global__ void __launch_bounds__(512, 1)
+template <int LOGC, class S, bool LIFT>
+__global__ void __launch_bounds__(S::T, 1)
     k_ntt_inv_cluster(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
                       const __grid_constant__ vkcu_lift lift) {
-  using S = SubShape;
-  using K = Cols<LOGC>;
+  using K = Cols<LOGC, S>;
   extern __shared__ u64 sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -157,17 +159,16 @@ __global__ void __launch_bounds__(512, 1)
     inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
     inv_last_smem<S>(sm, t, tw_mult);
     cl.sync();
-    col_inv_out<LOGC, LIFT>(reinterpret_cast<u64*>(job.out), sm, cl, rank, t, &lift);
+    col_inv_out<LOGC, S, LIFT>(reinterpret_cast<u64*>(job.out), sm, cl, rank, t, &lift);
   }
   cl.sync();
 }
 
-template <int LOGC, bool LIFT>
-__global__ void __launch_bounds__(512, 1)
+template <int LOGC, class S, bool LIFT>
+__global__ void __launch_bounds__(S::T, 1)
     k_polymul_cluster(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one,
                       const __grid_constant__ vkcu_lift lift) {
-  using S = SubShape;
-  using K = Cols<LOGC>;
+  using K = Cols<LOGC, S>;
   extern __shared__ u64 sm[];
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
@@ -184,7 +185,7 @@ __global__ void __launch_bounds__(512, 1)
 #pragma unroll 1
     for (int ph = 0; ph < 2; ph++) {
       cl.sync();
-      col_fwd<LOGC>(reinterpret_cast<const u64*>(ph ? job.a : job.b), sm, cl, rank, t);
+      col_fwd<LOGC, S>(reinterpret_cast<const u64*>(ph ? job.a : job.b), sm, cl, rank, t);
       cl.sync();
       fwd_first_smem<S>(sm, t, tw_mult);
       fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
@@ -208,29 +209,33 @@ __global__ void __launch_bounds__(512, 1)
     inv_passes<S>(sm, t, tw_mult, S::HEAD);
     inv_last_smem<S>(sm, t, tw_mult);
     cl.sync();
-    col_inv_out<LOGC, LIFT>(reinterpret_cast<u64*>(job.c), sm, cl, rank, t, &lift);
+    col_inv_out<LOGC, S, LIFT>(reinterpret_cast<u64*>(job.c), sm, cl, rank, t, &lift);
   }
   cl.sync();
 }
 
 // The kernel is a template argument so that each kernel gets its own
 // one-time attribute set-up (forward and inverse kernels share a signature).
-template <int LOGC, auto kern, class... Args>
+// The clusters are spread over SMs: a cluster of small CTAs would otherwise
+// be packed onto few SMs.
+template <int LOGC, class S, auto kern, class... Args>
 static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   constexpr int C = 1 << LOGC;
   static std::atomic<unsigned> prepared{0};
-  if (const int e = prepare(kern, SubShape::SMEM_BYTES, prepared)) return e;
+  if (const int e = prepare(kern, S::SMEM_BYTES, prepared)) return e;
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = C;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(SubShape::T);
-  cfg.dynamicSmemBytes = SubShape::SMEM_BYTES;
+  attr[1].id = cudaLaunchAttributeClusterSchedulingPolicyPreference;
+  attr[1].val.clusterSchedulingPolicyPreference = cudaClusterSchedulingPolicySpread;
+  cfg.blockDim = dim3(S::T);
+  cfg.dynamicSmemBytes = S::SMEM_BYTES;
   cfg.stream = st;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   cfg.gridDim = dim3(C);
   int max_clusters = 0;
   cudaError_t e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
@@ -243,41 +248,51 @@ static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   return (int)e;
 }
 
-int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc) {
-  switch (logc) {
-    case 1: return launch_cluster<1, k_ntt_fwd_cluster<1>>(st, njobs, jobs, njobs, one);
-    case 2: return launch_cluster<2, k_ntt_fwd_cluster<2>>(st, njobs, jobs, njobs, one);
-    case 3: return launch_cluster<3, k_ntt_fwd_cluster<3>>(st, njobs, jobs, njobs, one);
-    default: return (int)cudaErrorInvalidValue;
+// Sub-blocks of 2^10 / 2^11 words (16 per thread) for n = 2^13 / 2^14 on 8 CTAs.
+using Small10 = Shape<10, 16>;
+using Small11 = Shape<11, 16>;
+
+// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 10 / 11 with logc = 3).
+#define VK_CLUSTER_SHAPES(X)                                 \
+  switch (logc * 32 + logs) {                                \
+    case 1 * 32 + 14: return X(1, SubShape);                 \
+    case 2 * 32 + 14: return X(2, SubShape);                 \
+    case 3 * 32 + 14: return X(3, SubShape);                 \
+    case 3 * 32 + 10: return X(3, Small10);                  \
+    case 3 * 32 + 11: return X(3, Small11);                  \
+    default: return (int)cudaErrorInvalidValue;              \
   }
+
+int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs) {
+#define X(L, S) launch_cluster<L, S, k_ntt_fwd_cluster<L, S>>(st, njobs, jobs, njobs, one)
+  VK_CLUSTER_SHAPES(X)
+#undef X
 }
 
-int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs,
                 const vkcu_lift* lift) {
   const vkcu_lift l = lift ? *lift : vkcu_lift{};
-  switch (logc * 2 + (lift ? 1 : 0)) {
-    case 2: return launch_cluster<1, k_ntt_inv_cluster<1, false>>(st, njobs, jobs, njobs, one, l);
-    case 3: return launch_cluster<1, k_ntt_inv_cluster<1, true>>(st, njobs, jobs, njobs, one, l);
-    case 4: return launch_cluster<2, k_ntt_inv_cluster<2, false>>(st, njobs, jobs, njobs, one, l);
-    case 5: return launch_cluster<2, k_ntt_inv_cluster<2, true>>(st, njobs, jobs, njobs, one, l);
-    case 6: return launch_cluster<3, k_ntt_inv_cluster<3, false>>(st, njobs, jobs, njobs, one, l);
-    case 7: return launch_cluster<3, k_ntt_inv_cluster<3, true>>(st, njobs, jobs, njobs, one, l);
-    default: return (int)cudaErrorInvalidValue;
+  if (lift) {
+#define X(L, S) launch_cluster<L, S, k_ntt_inv_cluster<L, S, true>>(st, njobs, jobs, njobs, one, l)
+    VK_CLUSTER_SHAPES(X)
+#undef X
   }
+#define X(L, S) launch_cluster<L, S, k_ntt_inv_cluster<L, S, false>>(st, njobs, jobs, njobs, one, l)
+  VK_CLUSTER_SHAPES(X)
+#undef X
 }
 
-int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
+int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc, int logs,
                  const vkcu_lift* lift) {
   const vkcu_lift l = lift ? *lift : vkcu_lift{};
-  switch (logc * 2 + (lift ? 1 : 0)) {
-    case 2: return launch_cluster<1, k_polymul_cluster<1, false>>(st, njobs, jobs, njobs, one, l);
-    case 3: return launch_cluster<1, k_polymul_cluster<1, true>>(st, njobs, jobs, njobs, one, l);
-    case 4: return launch_cluster<2, k_polymul_cluster<2, false>>(st, njobs, jobs, njobs, one, l);
-    case 5: return launch_cluster<2, k_polymul_cluster<2, true>>(st, njobs, jobs, njobs, one, l);
-    case 6: return launch_cluster<3, k_polymul_cluster<3, false>>(st, njobs, jobs, njobs, one, l);
-    case 7: return launch_cluster<3, k_polymul_cluster<3, true>>(st, njobs, jobs, njobs, one, l);
-    default: return (int)cudaErrorInvalidValue;
+  if (lift) {
+#define X(L, S) launch_cluster<L, S, k_polymul_cluster<L, S, true>>(st, njobs, jobs, njobs, one, l)
+    VK_CLUSTER_SHAPES(X)
+#undef X
   }
+#define X(L, S) launch_cluster<L, S, k_polymul_cluster<L, S, false>>(st, njobs, jobs, njobs, one, l)
+  VK_CLUSTER_SHAPES(X)
+#undef X
 }
 
 }  // namespace vk

@@ -582,11 +582,12 @@ int inv_cta_lift(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkc
                  const vkcu_lift& lift);
 int poly_cta_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
                   int variant, const vkcu_lift& lift);
-// cluster of 2^logc CTAs, n = 2^(14 + logc)
-int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
-int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,
+// cluster of 2^logc CTAs with sub-blocks of 2^logs words, n = 2^(logc + logs):
+// logs = 14 for n = 2^15 .. 2^17; logc = 3 with logs = 10 / 11 for n = 2^13 / 2^14
+int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs);
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs,
                 const vkcu_lift* lift = nullptr);
-int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
+int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc, int logs,
                  const vkcu_lift* lift = nullptr);
 
 // Opts `kernel` into `smem` bytes of dynamic shared memory.  The attribute
