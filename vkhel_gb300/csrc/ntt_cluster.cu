@@ -17,8 +17,8 @@
 //             column from the C CTAs over DSMEM and runs the last log2 C
 //             stages with n^-1 folded in, writing global memory coalesced.
 //
-// The sub-block is 2^14 words (n = 2^15 .. 2^17, one CTA per SM), or 2^10 /
-// 2^11 words for n = 2^13 / 2^14 split over 8 CTAs when there are too few
+// The sub-block is 2^14 words (n = 2^15 .. 2^17, one CTA per SM), or 2^9 ..
+// 2^11 words for n = 2^12 .. 2^14 split over 8 CTAs when there are too few
 // jobs to fill the GPU with one CTA per job (single calls).
 //
 // Cluster barriers separate the phases: before a column pass writes another
@@ -248,16 +248,18 @@ static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   return (int)e;
 }
 
-// Sub-blocks of 2^10 / 2^11 words (16 per thread) for n = 2^13 / 2^14 on 8 CTAs.
+// Sub-blocks of 2^9 .. 2^11 words (16 per thread) for n = 2^12 .. 2^14 on 8 CTAs.
+using Small9 = Shape<9, 16>;
 using Small10 = Shape<10, 16>;
 using Small11 = Shape<11, 16>;
 
-// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 10 / 11 with logc = 3).
+// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 9 .. 11 with logc = 3).
 #define VK_CLUSTER_SHAPES(X)                                 \
   switch (logc * 32 + logs) {                                \
     case 1 * 32 + 14: return X(1, SubShape);                 \
     case 2 * 32 + 14: return X(2, SubShape);                 \
     case 3 * 32 + 14: return X(3, SubShape);                 \
+    case 3 * 32 + 9: return X(3, Small9);                    \
     case 3 * 32 + 10: return X(3, Small10);                  \
     case 3 * 32 + 11: return X(3, Small11);                  \
     default: return (int)cudaErrorInvalidValue;              \
