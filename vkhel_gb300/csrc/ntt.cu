@@ -142,10 +142,11 @@ static int simple(cudaStream_t st, bool inverse, const vkcu_ntt_job* jobs, int n
   const int threads = n / 2 < 32 ? 32 : (n / 2 > 512 ? 512 : n / 2);
   const int smem = n * 8;
   auto kern = inverse ? k_ntt_inv_simple : k_ntt_fwd_simple;
-  // opted in once per device for the largest n this path takes (2^14)
-  static std::atomic<unsigned> prepared_fwd{0}, prepared_inv{0};
-  if (int e = prepare(kern, (1 << kMaxCta) * 8, inverse ? prepared_inv : prepared_fwd)) return e;
-  const int grid = grid_for(kern, threads, smem, njobs, sms);
+  // threads and shared memory depend on n: one set-up per direction and degree
+  static KernelSetup setups[2][kMaxCta + 1];
+  int per_sm = 1;
+  if (int e = setup_cta(kern, threads, smem, setups[inverse ? 1 : 0][log_n], &per_sm)) return e;
+  const int grid = grid_from(per_sm, njobs, sms);
   kern<<<grid, threads, smem, st>>>(jobs, njobs, one, log_n);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();

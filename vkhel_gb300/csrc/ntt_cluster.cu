@@ -221,8 +221,7 @@ __global__ void __launch_bounds__(S::T, 1)
 template <int LOGC, class S, auto kern, class... Args>
 static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   constexpr int C = 1 << LOGC;
-  static std::atomic<unsigned> prepared{0};
-  if (const int e = prepare(kern, S::SMEM_BYTES, prepared)) return e;
+  static KernelSetup setup;  // resident clusters per device
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -237,10 +236,17 @@ static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   cfg.attrs = attr;
   cfg.numAttrs = 2;
   cfg.gridDim = dim3(C);
-  int max_clusters = 0;
-  cudaError_t e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
-  if (e != cudaSuccess) return (int)e;
-  if (max_clusters < 1) return (int)cudaErrorInvalidConfiguration;
+  const int dev = current_device();
+  const bool cached = dev >= 0 && dev < 32;
+  int max_clusters = cached ? setup.per_dev[dev].load(std::memory_order_acquire) : 0;
+  cudaError_t e = cudaSuccess;
+  if (max_clusters < 1) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BYTES);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
+    if (e != cudaSuccess) return (int)e;
+    if (max_clusters < 1) return (int)cudaErrorInvalidConfiguration;
+    if (cached) setup.per_dev[dev].store(max_clusters, std::memory_order_release);
+  }
   const int nclusters = njobs < max_clusters ? njobs : max_clusters;
   cfg.gridDim = dim3(nclusters * C);
   e = cudaLaunchKernelEx(&cfg, kern, args...);

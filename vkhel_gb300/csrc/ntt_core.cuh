@@ -590,25 +590,44 @@ int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu
 int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc, int logs,
                  const vkcu_lift* lift = nullptr);
 
-// Opts `kernel` into `smem` bytes of dynamic shared memory.  The attribute
-// is per device, so it is set once per device (bit d of `done`; devices
-// beyond 31 set it on every call).
-template <class K>
-static int prepare(K kernel, int smem, std::atomic<unsigned>& done) {
+// Launch set-up of one kernel, per device: the dynamic shared-memory opt-in
+// and the occupancy figure its grid is sized from (resident blocks per SM,
+// or resident clusters), both fixed for a kernel on a device, so they are
+// computed once per device instead of on every launch (devices beyond 31
+// recompute every time).
+struct KernelSetup {
+  std::atomic<int> per_dev[32];
+};
+
+__host__ inline int current_device() {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
-  const unsigned bit = dev >= 0 && dev < 32 ? 1u << dev : 0u;
-  if (bit && (done.load(std::memory_order_acquire) & bit)) return 0;
-  const int e = (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (!e && bit) done.fetch_or(bit, std::memory_order_release);
-  return e;
+  return cudaGetDevice(&dev) == cudaSuccess ? dev : -1;
 }
 
+// Opts `kernel` into `smem` bytes of dynamic shared memory and returns its
+// resident blocks per SM for `threads` threads (at least 1) in *per_sm.
 template <class K>
-static int grid_for(K kernel, int threads, int smem, long work, int sms) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
-    per_sm = 1;
+static int setup_cta(K kernel, int threads, int smem, KernelSetup& ks, int* per_sm) {
+  const int dev = current_device();
+  const bool cached = dev >= 0 && dev < 32;
+  if (cached) {
+    const int v = ks.per_dev[dev].load(std::memory_order_acquire);
+    if (v > 0) {
+      *per_sm = v;
+      return 0;
+    }
+  }
+  const int e = (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e) return e;
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem) != cudaSuccess || b < 1) b = 1;
+  if (cached) ks.per_dev[dev].store(b, std::memory_order_release);
+  *per_sm = b;
+  return 0;
+}
+
+// A persistent grid: one wave of resident blocks, or fewer when there is less work.
+__host__ inline int grid_from(int per_sm, long work, int sms) {
   const long cap = (long)per_sm * (sms > 0 ? sms : 1);
   return (int)(work < cap ? work : cap);
 }

@@ -10,9 +10,10 @@ static int launch_lift(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, co
                        const vkcu_lift& lift) {
   using S = Shape<LOGN, E, U>;
   auto kern = k_polymul<LOGN, E, U, true>;
-  static std::atomic<unsigned> prepared{0};
-  if (const int e = prepare(kern, S::SMEM_BYTES, prepared)) return e;
-  const int grid = grid_for(kern, S::T, S::SMEM_BYTES, (long)njobs, sms);
+  static KernelSetup setup;
+  int per_sm = 1;
+  if (const int e = setup_cta(kern, S::T, S::SMEM_BYTES, setup, &per_sm)) return e;
+  const int grid = grid_from(per_sm, (long)njobs, sms);
   kern<<<grid, S::T, S::SMEM_BYTES, st>>>(jobs, njobs, one, lift);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
