@@ -142,10 +142,11 @@ static int simple(cudaStream_t st, bool inverse, const vkcu_ntt_job* jobs, int n
   const int threads = n / 2 < 32 ? 32 : (n / 2 > 512 ? 512 : n / 2);
   const int smem = n * 8;
   auto kern = inverse ? k_ntt_inv_simple : k_ntt_fwd_simple;
-  // threads and shared memory depend on n: one set-up per direction and degree
+  // threads and shared memory depend on n: one occupancy per direction and
+  // degree; the kernel's shared-memory limit is the largest n (2^14) always
   static KernelSetup setups[2][kMaxCta + 1];
   int per_sm = 1;
-  if (int e = setup_cta(kern, threads, smem, setups[inverse ? 1 : 0][log_n], &per_sm)) return e;
+  if (int e = setup_cta(kern, threads, smem, setups[inverse ? 1 : 0][log_n], &per_sm, (1 << kMaxCta) * 8)) return e;
   const int grid = grid_from(per_sm, njobs, sms);
   kern<<<grid, threads, smem, st>>>(jobs, njobs, one, log_n);
   vkcu_count_launches(1);

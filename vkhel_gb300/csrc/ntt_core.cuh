@@ -604,10 +604,12 @@ __host__ inline int current_device() {
   return cudaGetDevice(&dev) == cudaSuccess ? dev : -1;
 }
 
-// Opts `kernel` into `smem` bytes of dynamic shared memory and returns its
-// resident blocks per SM for `threads` threads (at least 1) in *per_sm.
+// Opts `kernel` into `smem_limit` (default: `smem`) bytes of dynamic shared
+// memory -- the attribute belongs to the kernel, so a kernel launched with
+// several sizes is opted into the largest -- and returns its resident blocks
+// per SM for `threads` threads and `smem` bytes (at least 1) in *per_sm.
 template <class K>
-static int setup_cta(K kernel, int threads, int smem, KernelSetup& ks, int* per_sm) {
+static int setup_cta(K kernel, int threads, int smem, KernelSetup& ks, int* per_sm, int smem_limit = 0) {
   const int dev = current_device();
   const bool cached = dev >= 0 && dev < 32;
   if (cached) {
@@ -617,7 +619,8 @@ static int setup_cta(K kernel, int threads, int smem, KernelSetup& ks, int* per_
       return 0;
     }
   }
-  const int e = (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const int e = (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          smem_limit > smem ? smem_limit : smem);
   if (e) return e;
   int b = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem) != cudaSuccess || b < 1) b = 1;
