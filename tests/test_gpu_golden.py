@@ -63,3 +63,13 @@ def test_reference_transform_in_place(vk, ctx):
         v = vk.Vector(ctx, _ints(op["a"]))
         getattr(vk, op["op"])(v, v, t)
         np.testing.assert_array_equal(v.map_read(), _ints(op["expected"]))
+
+
+@pytest.mark.gpu
+def test_vector_dbgprint_matches_reference_format(vk, ctx, capfd):
+    # src/vector.c:237-247: the words, ", "-separated, then a newline
+    import ctypes
+    v = vk.Vector(ctx, np.array([3, 0, (1 << 64) - 1, 42], dtype=np.uint64))
+    vk.lib().vkhel_vector_dbgprint(v.ptr)
+    ctypes.CDLL(None).fflush(None)
+    assert capfd.readouterr().out == f"3, 0, {(1 << 64) - 1}, 42\n"

@@ -125,3 +125,23 @@ def test_workload_prime_rule():
     for q in qs:
         w = workloads.root_for(16384, q)
         assert pow(w, 16384, q) == q - 1
+
+
+def _flush_c_stdout():
+    import ctypes
+    ctypes.CDLL(None).fflush(None)
+
+
+def test_tables_dbgprint_matches_reference_format(vk, oracle, capfd):
+    # src/ntt_tables.c:46-63: header line, then the roots and the inverse roots
+    n, q = 16, 2251799813685313
+    w = 110968848420801
+    t = vk.NttTables(n, q, w)
+    vk.lib().vkhel_ntt_tables_dbgprint(t.ptr)
+    _flush_c_stdout()
+    out = capfd.readouterr().out
+    ref = oracle.tables(n, q, w)
+    expect = (f"ntt_tables: (n={n} q={q} w={w})\n"
+              f"\troots_of_unity: {', '.join(str(int(x)) for x in ref['roots'])}\n"
+              f"\tinv_roots_of_unity: {', '.join(str(int(x)) for x in ref['inv_roots'])}\n")
+    assert out == expect
