@@ -70,3 +70,34 @@ def test_c_program_replays_reference_golden_vectors(vk, tmp_path):
     r = subprocess.run([exe, cases], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "35 cases, 0 failed" in r.stdout
+
+
+EXT_SRC = os.path.join(ROOT, "tests", "c", "test_vkhel_ext.c")
+
+
+def _build_ext(tmp_path):
+    from vkhel_gb300 import LIB_PATH
+    exe = str(tmp_path / "test_vkhel_ext")
+    libdir = os.path.dirname(LIB_PATH)
+    subprocess.run(["gcc", "-std=gnu11", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include", "vkhel"),
+                    EXT_SRC, "-o", exe, "-L", libdir, "-lvkhel", f"-Wl,-rpath,{libdir}"], check=True)
+    return exe
+
+
+def _ext_args(n=1024):
+    from vkhel_gb300 import workloads
+    qs = workloads.ntt_primes(n, 3)
+    return [str(n)] + [str(x) for q in qs for x in (q, workloads.root_for(n, q))]
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_c_extension_program_links_and_reports_no_device(vk, tmp_path):
+    r = subprocess.run([_build_ext(tmp_path)] + _ext_args(), capture_output=True, text=True)
+    assert r.returncode == 77 and "no CUDA device" in r.stdout
+
+
+@pytest.mark.gpu
+def test_c_extension_program_checks_pass(vk, tmp_path):
+    r = subprocess.run([_build_ext(tmp_path)] + _ext_args(), capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 checks failed" in r.stdout
