@@ -506,8 +506,8 @@ def standalone_ops(vk, ctx, torch, orc, words=1 << 27, reps=5):
     modulus, uniform operands, seed 7): device time per call (CUDA events on
     the context stream; the call's own synchronisation is inside the
     bracket) and GB/s of its algorithmic bytes against the HBM copy peak; and
-    single-call forward / inverse transforms (n = 2^12, 2^14 and 2^17) with
-    their latency.  Spot-checked against the oracle."""
+    single-call forward / inverse transforms (n = 2^12, 2^14, 2^16 and 2^17)
+    with their latency.  Spot-checked against the oracle."""
     from vkhel_gb300 import workloads
     rng = np.random.default_rng(7)
     q = (1 << 61) - 1
@@ -527,7 +527,7 @@ def standalone_ops(vk, ctx, torch, orc, words=1 << 27, reps=5):
     got = r.download(k)
     ref = orc.elemmod(a.download(k), 65537, q)
     assert np.array_equal(got, ref), "standalone elemmod differs from the oracle"
-    for log_n in (12, 14, 17):
+    for log_n in (12, 14, 16, 17):
         n = 1 << log_n
         qq = workloads.ntt_primes(n, 1)[0]
         t = vk.NttTables(n, qq, workloads.root_for(n, qq))

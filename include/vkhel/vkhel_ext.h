@@ -227,7 +227,7 @@ void vkhel_elem_batch_destroy(struct vkhel_elem_batch *batch);
  * of which one to launch is read once per process from $VKHEL_TUNE_TABLE or
  * from tuning/gb300.txt beside the package (written by vkhel_gb300.autotune).
  * Family VKHEL_TUNE_BATCH, log_n 0: 1 = run the degree classes of a batch on
- * concurrent streams; log_n 1: 1 = never split a few n = 2^12 .. 2^14 jobs
+ * concurrent streams; log_n 1: 1 = never split a few n = 2^12 .. 2^16 jobs
  * (at most one per 8 SMs, e.g. a single call) over 8-CTA clusters (the
  * default, 0, splits them). */
 enum vkhel_tune_family {

@@ -50,10 +50,10 @@ def test_every_variant_matches_oracle(vk, ctx, oracle, log_n):
         L.vkhel_tune_set(3, 1, split)
 
 
-@pytest.mark.parametrize("log_n", [12, 13, 14])
+@pytest.mark.parametrize("log_n", [12, 13, 14, 15, 16])
 @pytest.mark.parametrize("split", [0, 1])
 def test_single_calls_split_or_not_are_exact(vk, ctx, oracle, log_n, split):
-    """A single call of n = 2^12 .. 2^14 runs on an 8-CTA cluster (2^9 .. 2^11-word
+    """A single call of n = 2^12 .. 2^16 runs on an 8-CTA cluster (2^9 .. 2^13-word
     sub-blocks) unless the split is switched off; both give the oracle's words."""
     L = vk.lib()
     n = 1 << log_n

@@ -194,12 +194,12 @@ static bool jobs_aligned(const vkcu_ntt_job* jobs, const vkcu_ntt_job* one) {
   return jobs != nullptr || (aligned32(one->in) && aligned32(one->out));
 }
 
-// Few jobs of n = 2^12 .. 2^14 (at most one per 8 SMs, e.g. a single call):
-// each runs on a cluster of 8 CTAs with 2^9 .. 2^11-word sub-blocks instead
-// of one CTA, so it uses 8 SMs.  Tuning entry (family 3, log_n 1) = 1 turns
-// this off.
+// Few jobs of n = 2^12 .. 2^16 (at most one per 8 SMs, e.g. a single call):
+// each runs on a cluster of 8 CTAs with 2^9 .. 2^13-word sub-blocks instead
+// of one CTA (n <= 2^14) or a cluster of 2 / 4 CTAs (n = 2^15 / 2^16), so it
+// uses 8 SMs.  Tuning entry (family 3, log_n 1) = 1 turns this off.
 static bool split_small(int njobs, uint32_t log_n, int sms) {
-  return log_n >= 12 && log_n <= 14 && (long)njobs * 8 <= (long)sms && vkh_variant(3, 1) == 0;
+  return log_n >= 12 && log_n <= 16 && (long)njobs * 8 <= (long)sms && vkh_variant(3, 1) == 0;
 }
 
 extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,

@@ -18,8 +18,8 @@
 //             stages with n^-1 folded in, writing global memory coalesced.
 //
 // The sub-block is 2^14 words (n = 2^15 .. 2^17, one CTA per SM), or 2^9 ..
-// 2^11 words for n = 2^12 .. 2^14 split over 8 CTAs when there are too few
-// jobs to fill the GPU with one CTA per job (single calls).
+// 2^13 words for n = 2^12 .. 2^16 split over 8 CTAs when there are too few
+// jobs to fill the GPU otherwise (single calls, small server micro-batches).
 //
 // Cluster barriers separate the phases: before a column pass writes another
 // CTA's shared memory (its owner has finished reading it), after it (the
@@ -254,12 +254,15 @@ static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   return (int)e;
 }
 
-// Sub-blocks of 2^9 .. 2^11 words (16 per thread) for n = 2^12 .. 2^14 on 8 CTAs.
+// Sub-blocks of 2^9 .. 2^13 words for n = 2^12 .. 2^16 on 8 CTAs (16 words
+// per thread; 32 at 2^13, so that 256 threads fit the register file).
 using Small9 = Shape<9, 16>;
 using Small10 = Shape<10, 16>;
 using Small11 = Shape<11, 16>;
+using Small12 = Shape<12, 16>;
+using Small13 = Shape<13, 32>;
 
-// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 9 .. 11 with logc = 3).
+// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 9 .. 13 with logc = 3).
 #define VK_CLUSTER_SHAPES(X)                                 \
   switch (logc * 32 + logs) {                                \
     case 1 * 32 + 14: return X(1, SubShape);                 \
@@ -268,6 +271,8 @@ using Small11 = Shape<11, 16>;
     case 3 * 32 + 9: return X(3, Small9);                    \
     case 3 * 32 + 10: return X(3, Small10);                  \
     case 3 * 32 + 11: return X(3, Small11);                  \
+    case 3 * 32 + 12: return X(3, Small12);                  \
+    case 3 * 32 + 13: return X(3, Small13);                  \
     default: return (int)cudaErrorInvalidValue;              \
   }
 
