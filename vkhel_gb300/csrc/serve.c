@@ -24,9 +24,6 @@
  */
 #include <errno.h>
 #include <pthread.h>
-#ifdef __linux__
-#include <sys/prctl.h>
-#endif
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
@@ -235,11 +232,6 @@ static void finish_slot(struct vkhel_server *s, struct srv_slot *sl, int status)
 static void *scheduler(void *arg) {
 	struct vkhel_server *s = arg;
 	vkcu_set_device(s->ctx->device);
-#ifdef __linux__
-	/* the completion polls sleep 10 us; the default 50 us timer slack would
-	 * stretch each to about 60 us and add that to every request's latency */
-	prctl(PR_SET_TIMERSLACK, 1000UL, 0, 0, 0);
-#endif
 	for (;;) {
 		int progressed = 0;
 		/* completions */
@@ -300,7 +292,7 @@ static void *scheduler(void *arg) {
 				pthread_mutex_unlock(&s->mu);
 			} else {
 				pthread_mutex_unlock(&s->mu);
-				const struct timespec ts = {0, 10000}; /* 10 us between completion polls */
+				const struct timespec ts = {0, 20000}; /* 20 us between completion polls */
 				nanosleep(&ts, NULL);
 			}
 		} else {
