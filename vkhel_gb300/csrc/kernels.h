@@ -53,6 +53,8 @@ int vkcu_stream_destroy(void *stream);
 int vkcu_pool_create(int device, void **pool);
 int vkcu_pool_destroy(void *pool);
 int vkcu_pool_independent_streams(void *pool);
+/* fn(arg) on a driver thread after the stream's earlier work (no CUDA calls in fn). */
+int vkcu_launch_host_func(void *stream, void (*fn)(void *), void *arg);
 /* Profiler ranges (NVTX) around entry points. */
 void vkcu_range_push(const char *name);
 void vkcu_range_pop(void);

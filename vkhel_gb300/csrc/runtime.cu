@@ -155,6 +155,12 @@ extern "C" int vkcu_stream_wait(void* stream, void* ev) {
 }
 
 // 0 = completed, 1 = not yet, anything else = CUDA error
+// Runs fn(arg) on a driver thread once the stream's earlier work has
+// completed (fn must make no CUDA calls).
+extern "C" int vkcu_launch_host_func(void* stream, void (*fn)(void*), void* arg) {
+  return (int)cudaLaunchHostFunc((cudaStream_t)stream, fn, arg);
+}
+
 extern "C" int vkcu_event_query(void* ev) {
   const cudaError_t r = cudaEventQuery((cudaEvent_t)ev);
   if (r == cudaSuccess) return 0;

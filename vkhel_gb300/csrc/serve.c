@@ -15,8 +15,10 @@
  *     downloads results on the output stream; the three streams are chained
  *     by events, so while one micro-batch computes the next is uploaded and
  *     the previous one downloaded;
- *   - polls completion events, releases memory and wakes waiters; requests
- *     that arrive while others run join the next micro-batch.
+ *   - a stream callback after each micro-batch's downloads completes its
+ *     requests, releases their memory and wakes waiters and the scheduler
+ *     (slower event polls catch a failed stream); requests that arrive while
+ *     others run join the next micro-batch.
  * Every limb product is computed exactly as in the plain API, so a request's
  * result is the same alone and in any mix.  Latency = completion - submission
  * (monotonic clock), recorded per request.  All device work happens on the
@@ -47,8 +49,14 @@ struct srv_req {
 	uint64_t dev_bytes;
 };
 
+struct vkhel_server;
+
 struct srv_slot {
+	struct vkhel_server *srv;
 	int busy;
+	int done;                 /* finished (by its callback or, on error, by a poll) */
+	uint64_t launches;        /* micro-batches enqueued on this slot */
+	uint64_t callbacks;       /* completion callbacks run (stream order = launch order) */
 	void *ev_in, *ev_comp, *ev_done;
 	vkcu_poly_job *host_poly; /* pinned */
 	vkcu_ntt_job *host_ntt;   /* pinned, 3 per job */
@@ -97,6 +105,25 @@ static uint64_t req_bytes(const struct srv_req *r) {
 static int cmp_job_log_n(const void *x, const void *y) {
 	const uint64_t a = *(const uint64_t *) x, b = *(const uint64_t *) y;
 	return (a > b) - (a < b);
+}
+
+static void finish_slot(struct vkhel_server *s, struct srv_slot *sl, int status);
+
+/* Stream callback after a micro-batch's downloads: completes its requests at
+ * once (no CUDA calls here) and wakes the scheduler for the freed slot.  If
+ * the stream failed, the callback may never run; the scheduler's slower
+ * event polls then finish the slot with an error. */
+static void slot_done_cb(void *arg) {
+	struct srv_slot *sl = arg;
+	struct vkhel_server *s = sl->srv;
+	pthread_mutex_lock(&s->mu);
+	/* only the callback of the slot's current launch finishes it */
+	if (++sl->callbacks == sl->launches && sl->busy && !sl->done) {
+		sl->done = 1;
+		finish_slot(s, sl, 0);
+	}
+	pthread_cond_broadcast(&s->cv_work);
+	pthread_mutex_unlock(&s->mu);
 }
 
 /* Enqueue one micro-batch on the server streams (called without the lock). */
@@ -195,6 +222,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 		r->dev = NULL;
 	}
 	vkcu_event_record(sl->ev_done, s->s_out);
+	vkcu_launch_host_func(s->s_out, slot_done_cb, sl);
 	free(keys);
 	free(tmp);
 	vkcu_range_pop();
@@ -234,18 +262,25 @@ static void *scheduler(void *arg) {
 	vkcu_set_device(s->ctx->device);
 	for (;;) {
 		int progressed = 0;
-		/* completions */
+		/* micro-batches complete through their stream callbacks; these polls
+		 * only catch a failed stream, whose callback may never run */
 		for (uint32_t k = 0; k < s->nslots; k++) {
 			struct srv_slot *sl = &s->slots[k];
-			if (!sl->busy)
+			pthread_mutex_lock(&s->mu);
+			const int live = sl->busy && !sl->done;
+			pthread_mutex_unlock(&s->mu);
+			if (!live)
 				continue;
 			const int q = vkcu_event_query(sl->ev_done);
-			if (q == 1)
+			if (q == 0 || q == 1) /* done (its callback finishes it) or still running */
 				continue;
 			pthread_mutex_lock(&s->mu);
-			finish_slot(s, sl, q == 0 ? 0 : VKHEL_ERR_DEVICE);
+			if (sl->busy && !sl->done) {
+				sl->done = 1;
+				finish_slot(s, sl, VKHEL_ERR_DEVICE);
+				progressed = 1;
+			}
 			pthread_mutex_unlock(&s->mu);
-			progressed = 1;
 		}
 		/* admission */
 		pthread_mutex_lock(&s->mu);
@@ -280,6 +315,8 @@ static void *scheduler(void *arg) {
 		}
 		if (free_slot && free_slot->nreqs) {
 			free_slot->busy = 1;
+			free_slot->done = 0;
+			free_slot->launches++;
 			pthread_mutex_unlock(&s->mu);
 			launch_slot(s, free_slot);
 			progressed = 1;
@@ -289,15 +326,20 @@ static void *scheduler(void *arg) {
 			if (inflight == 0) {
 				while (!s->q_head && !s->stop)
 					pthread_cond_wait(&s->cv_work, &s->mu);
-				pthread_mutex_unlock(&s->mu);
 			} else {
-				pthread_mutex_unlock(&s->mu);
-				const struct timespec ts = {0, 20000}; /* 20 us between completion polls */
-				nanosleep(&ts, NULL);
+				/* woken by a completion callback or a submission; the timeout
+				 * bounds how late a failed stream is noticed */
+				struct timespec dl;
+				clock_gettime(CLOCK_REALTIME, &dl);
+				dl.tv_nsec += 200000;
+				if (dl.tv_nsec >= 1000000000L) {
+					dl.tv_sec++;
+					dl.tv_nsec -= 1000000000L;
+				}
+				pthread_cond_timedwait(&s->cv_work, &s->mu, &dl);
 			}
-		} else {
-			pthread_mutex_unlock(&s->mu);
 		}
+		pthread_mutex_unlock(&s->mu);
 	}
 	return NULL;
 }
@@ -340,6 +382,7 @@ struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg) 
 	const uint64_t cap = (uint64_t) s->max_limbs + 64;
 	for (uint32_t k = 0; !e && k < s->nslots; k++) {
 		struct srv_slot *sl = &s->slots[k];
+		sl->srv = s;
 		sl->reqs = calloc(2 * cap, sizeof(*sl->reqs));
 		e = !sl->reqs;
 		if (!e)
