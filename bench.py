@@ -540,7 +540,35 @@ def standalone_ops(vk, ctx, torch, orc, words=1 << 27, reps=5):
     return out
 
 
+def transform_batch(vk, ctx, torch, orc, n=N, count=1024):
+    """1024 forward transforms of n = 16384 (one 60-bit prime, seed 8) as one
+    committed batch (CUDA graph), 256 MB of operands (above L2): transforms/s
+    against the live butterfly peak ((n/2) log2 n Shoup products each) and
+    HBM (16 n bytes each)."""
+    from vkhel_gb300 import workloads
+    rng = np.random.default_rng(8)
+    q = workloads.ntt_primes(n, 1)[0]
+    w = workloads.root_for(n, q)
+    t = vk.NttTables(n, q, w)
+    x_h = workloads.uniform(rng, q, count * n)
+    x, y = vk.Vector(ctx, x_h), vk.Vector(ctx, count * n)
+    bt = vk.Batch(ctx)
+    bt.add_transform([t] * count, x, y)
+    bt.commit(graph=True)
+    sec = _event_time(torch, ctx, bt.launch, 20)
+    assert np.array_equal(y.download(n), orc.forward(x_h[:n], n, q, w)[0]), "batched forward differs from the oracle"
+    bfly = count * (n // 2) * (n.bit_length() - 1)
+    peak_b, _ = ctx.measure_int_peak()
+    hbm = load_peaks()[0].get("hbm_gbs", 6800.0)
+    bt.close()
+    return {"workload": f"{count} forward transforms of n = {n}, 60-bit prime, seed 8 (graph replay)",
+            "transforms_per_s": count / sec, "ms_per_batch": sec * 1e3,
+            "gbfly_per_s": bfly / sec / 1e9, "int_frac": bfly / sec / peak_b,
+            "hbm_gbs": 16 * n * count / sec / 1e9, "hbm_frac": 16 * n * count / sec / 1e9 / hbm}
+
+
 EXTRAS = {"single_limb_batch": single_limb_batch, "ragged_batch": ragged_batch,
+          "transform_batch": transform_batch,
           "standalone_ops": standalone_ops,
           "lift_epilogue": lift_epilogue, "elementwise_batch": elementwise_batch,
           "device_twiddles": device_twiddles}

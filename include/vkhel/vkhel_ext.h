@@ -149,7 +149,7 @@ int vkhel_vector_polymul_noalloc(const struct vkhel_vector *a,
 		const struct vkhel_vector *b, struct vkhel_vector *result,
 		const struct vkhel_ntt_tables *ntt);
 
-/* ---- batched polynomial multiply ----
+/* ---- batched polynomial multiply and transforms ----
  * A batch is a fixed list of limb products, built once, committed (the job
  * table is uploaded and, with VKHEL_BATCH_GRAPH, the launch sequence is
  * captured in a CUDA graph), then launched any number of times.  Jobs of
@@ -171,6 +171,20 @@ int vkhel_batch_add_polymul(struct vkhel_batch *batch,
 int vkhel_batch_add_polymul_raw(struct vkhel_batch *batch,
 		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *b, uint64_t *c);
+/* Transforms of `limbs` limbs: limb k of `out` (n words at offset k n) =
+ * the forward or inverse transform of limb k of `in` with tables[k], equal
+ * to vkhel_vector_forward_transform / vkhel_vector_inverse_transform of that
+ * limb (in place when in == out).  An inverse may carry a centred-lift
+ * epilogue (steps, as vkhel_batch_add_polymul_lift; nsteps 0 for none). */
+enum vkhel_transform_direction {
+	VKHEL_TRANSFORM_FORWARD = 0,
+	VKHEL_TRANSFORM_INVERSE = 1
+};
+int vkhel_batch_add_transform(struct vkhel_batch *batch,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *in, struct vkhel_vector *out,
+		uint32_t direction, const struct vkhel_lift_step *steps,
+		uint32_t nsteps);
 /* vkhel_batch_add_polymul with a centred-lift epilogue on every limb. */
 int vkhel_batch_add_polymul_lift(struct vkhel_batch *batch,
 		struct vkhel_ntt_tables *const *tables, uint32_t limbs,

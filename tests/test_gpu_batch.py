@@ -95,3 +95,51 @@ def test_batch_rejects_bad_input(vk, ctx):
         batch.commit()  # empty
     with pytest.raises(vk.VkhelError):
         batch.launch()  # not committed
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_transforms_mixed_with_polymul(vk, ctx, oracle, graph):
+    """Forward and inverse transforms (in place and not, an inverse with a lift)
+    and polymuls of several degrees in one batch equal the oracle."""
+    rng = np.random.default_rng(31 + graph)
+    bt = vk.Batch(ctx)
+    checks = []
+    for log_n, limbs in [(2, 2), (8, 3), (12, 2), (14, 4), (15, 1), (16, 2), (18, 1), (13, 40)]:
+        n = 1 << log_n
+        qs = workloads.ntt_primes(n, limbs) if log_n > 2 else [113, 17][:limbs]
+        ws = [workloads.root_for(n, q) for q in qs]
+        tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+        x_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+        y_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+        x, y = vk.Vector(ctx, x_h), vk.Vector(ctx, y_h)
+        fwd_out = vk.Vector(ctx, limbs * n)
+        bt.add_transform(tabs, x, fwd_out)                                   # forward, out of place
+        bt.add_transform(tabs, y, y, inverse=True)                           # inverse, in place
+        lifted = vk.Vector(ctx, limbs * n)
+        bt.add_transform(tabs, x, lifted, inverse=True, lift=[("elemmod", 65537, 0)])
+        prod = vk.Vector(ctx, limbs * n)
+        bt.add_polymul(tabs, x, vk.Vector(ctx, y_h), prod)
+        checks.append((n, qs, ws, x_h, y_h, fwd_out, y, lifted, prod))
+    bt.commit(graph=graph)
+    bt.run()
+    for n, qs, ws, x_h, y_h, fwd_out, y, lifted, prod in checks:
+        f, i, l, p = fwd_out.download(), y.download(), lifted.download(), prod.download()
+        for k, (q, w) in enumerate(zip(qs, ws)):
+            s = slice(k * n, (k + 1) * n)
+            np.testing.assert_array_equal(f[s], oracle.forward(x_h[s], n, q, w)[0], err_msg=f"forward n={n}")
+            np.testing.assert_array_equal(i[s], oracle.inverse(y_h[s], n, q, w)[0], err_msg=f"inverse n={n}")
+            np.testing.assert_array_equal(l[s], oracle.elemmod(oracle.inverse(x_h[s], n, q, w)[0], 65537, q),
+                                          err_msg=f"lifted inverse n={n}")
+            np.testing.assert_array_equal(p[s], oracle.polymul(x_h[s], y_h[s], n, q, w)[0], err_msg=f"polymul n={n}")
+
+
+def test_batch_transform_rejects_bad_arguments(vk, ctx):
+    n = 1024
+    q = workloads.ntt_primes(n, 1)[0]
+    t = vk.NttTables(n, q, workloads.root_for(n, q))
+    x, y = vk.Vector(ctx, n), vk.Vector(ctx, n // 2)
+    bt = vk.Batch(ctx)
+    with pytest.raises(vk.VkhelError):
+        bt.add_transform([t], x, y)                                          # output too short
+    with pytest.raises(vk.VkhelError):
+        bt.add_transform([t], x, x, inverse=False, lift=[("elemmod", 3, 0)])  # lift on a forward

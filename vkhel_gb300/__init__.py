@@ -79,6 +79,7 @@ _SIGNATURES = [
     ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_lift", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp, vp, u32]),
+    ("vkhel_batch_add_transform", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, u32, vp, u32]),
     ("vkhel_debug_fail_allocations", ctypes.c_int, [u64, u64]),
     ("vkhel_server_cancel", ctypes.c_int, [vp, ctypes.c_int64]),
     ("vkhel_elem_batch_create", vp, [vp]),
@@ -441,6 +442,14 @@ class Batch:
         else:  # raw device pointers
             code = lib().vkhel_batch_add_polymul_raw(self.ptr, arr, len(tables), int(a), int(b), int(c))
         _status(self.ctx.ptr, code)
+
+    def add_transform(self, tables, inp, out, inverse=False, lift=None):
+        """Forward (or inverse, optionally with a lift) transform of every limb of inp into out."""
+        arr = (vp * len(tables))(*[t.ptr for t in tables])
+        self._keep.append((tables, inp, out))
+        steps, n = lift_steps(lift or [])
+        _status(self.ctx.ptr, lib().vkhel_batch_add_transform(self.ptr, arr, len(tables), inp.ptr, out.ptr,
+                                                              1 if inverse else 0, ctypes.addressof(steps), n))
 
     def commit(self, graph=True):
         _status(self.ctx.ptr, lib().vkhel_batch_commit(self.ptr, BATCH_GRAPH if graph else 0))

@@ -21,6 +21,7 @@
 #define MAX_CLASSES 32
 
 struct job_rec {
+	uint32_t kind;         /* VKH_JOB_* */
 	uint32_t log_n;
 	uint32_t needs_scratch;
 	uint32_t lift;         /* index into the batch's lift table, 0 = none */
@@ -90,12 +91,14 @@ static int lift_index(struct vkhel_batch *b, const vkcu_lift *l, uint32_t *idx) 
 	return VKHEL_OK;
 }
 
+/* Limb jobs of one call: a polymul (a, bb -> c) or a transform (a -> c, bb
+ * unused). */
 static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
-		const uint64_t *a, const uint64_t *bb, uint64_t *c, const vkcu_lift *lift) {
+		const uint64_t *a, const uint64_t *bb, uint64_t *c, const vkcu_lift *lift, uint32_t kind) {
 	struct vkhel_ctx *ctx = b->ctx;
 	if (b->committed)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch: already committed");
-	if (!tables || limbs == 0 || !a || !bb || !c)
+	if (!tables || limbs == 0 || !a || (kind == VKH_JOB_POLYMUL && !bb) || !c)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: bad arguments");
 	if (((uintptr_t) a | (uintptr_t) bb | (uintptr_t) c) & 31)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: pointers must be 32-byte aligned");
@@ -129,16 +132,17 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		struct job_rec *r = &b->recs[b->njobs++];
 		const uint32_t log_n = tables[k]->log_n;
 		const int fused = log_n >= 8 && log_n <= vkcu_max_fused_log_n();
-		const uint64_t *ak = a + (uint64_t) k * n, *bk = bb + (uint64_t) k * n;
+		const uint64_t *ak = a + (uint64_t) k * n, *bk = bb ? bb + (uint64_t) k * n : NULL;
 		uint64_t *ck = c + (uint64_t) k * n;
 		/* the fused kernel parks NTT(b) in c, which must not hold a */
 		const int overlap = ak < ck + n && ck < ak + n;
+		r->kind = kind;
 		r->log_n = log_n;
-		r->needs_scratch = !fused || overlap;
+		r->needs_scratch = kind == VKH_JOB_POLYMUL && (!fused || overlap);
 		r->lift = lift_id;
 		r->order = b->njobs - 1;
 		r->job.a = ak;
-		r->job.b = bk;
+		r->job.b = kind == VKH_JOB_POLYMUL ? bk : NULL;
 		r->job.c = ck;
 		r->job.scratch = ck;
 		r->job.tw = d->dev_set;
@@ -157,7 +161,7 @@ int vkhel_batch_add_polymul(struct vkhel_batch *b, struct vkhel_ntt_tables *cons
 	const uint64_t need = (uint64_t) limbs * tables[0]->n;
 	if (a->length < need || bb->length < need || c->length < need)
 		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors shorter than limbs * n");
-	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, NULL);
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, NULL, VKH_JOB_POLYMUL);
 }
 
 int vkhel_batch_add_polymul_lift(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
@@ -177,18 +181,44 @@ int vkhel_batch_add_polymul_lift(struct vkhel_batch *b, struct vkhel_ntt_tables 
 	const int st = vkh_lift_compile(b->ctx, steps, nsteps, 0, &lift);
 	if (st)
 		return st;
-	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, &lift);
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, &lift, VKH_JOB_POLYMUL);
+}
+
+int vkhel_batch_add_transform(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *in, struct vkhel_vector *out, uint32_t direction,
+		const struct vkhel_lift_step *steps, uint32_t nsteps) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add_transform: NULL batch");
+	if (!in || !out || !tables || !tables[0])
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add_transform: NULL argument");
+	if (in->ctx != b->ctx || out->ctx != b->ctx)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add_transform: vectors of another context");
+	if (direction != VKHEL_TRANSFORM_FORWARD && direction != VKHEL_TRANSFORM_INVERSE)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add_transform: unknown direction %u", direction);
+	if (nsteps && direction != VKHEL_TRANSFORM_INVERSE)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add_transform: an epilogue needs the inverse");
+	const uint64_t need = (uint64_t) limbs * tables[0]->n;
+	if (in->length < need || out->length < need)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add_transform: vectors shorter than limbs * n");
+	vkcu_lift lift;
+	const int st = vkh_lift_compile(b->ctx, steps, nsteps, 0, &lift);
+	if (st)
+		return st;
+	return add_jobs(b, tables, limbs, in->dev, NULL, out->dev, &lift,
+			direction == VKHEL_TRANSFORM_FORWARD ? VKH_JOB_FORWARD : VKH_JOB_INVERSE);
 }
 
 int vkhel_batch_add_polymul_raw(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *bb, uint64_t *c) {
 	if (!b)
 		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
-	return add_jobs(b, tables, limbs, a, bb, c, NULL);
+	return add_jobs(b, tables, limbs, a, bb, c, NULL, VKH_JOB_POLYMUL);
 }
 
 static int cmp_rec(const void *x, const void *y) {
 	const struct job_rec *a = x, *b = y;
+	if (a->kind != b->kind)
+		return (a->kind > b->kind) - (a->kind < b->kind);
 	if (a->log_n != b->log_n)
 		return (a->log_n > b->log_n) - (a->log_n < b->log_n);
 	if (a->lift != b->lift)
@@ -206,8 +236,13 @@ int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, cons
 	for (uint32_t k = 0; k < nclasses; k++) {
 		const struct vkh_job_class *cl = &classes[k];
 		const vkcu_lift *lift = lifts && cl->lift ? &lifts[cl->lift] : NULL;
+		const vkcu_ntt_job *tj = dev_ntt + 3 * (size_t) cl->first;
 		int e;
-		if (cl->fused) {
+		if (cl->kind == VKH_JOB_FORWARD) {
+			e = vkcu_ntt_forward(stream, tj, (int) cl->count, NULL, cl->log_n, sms);
+		} else if (cl->kind == VKH_JOB_INVERSE) {
+			e = vkcu_ntt_inverse_lift(stream, tj, (int) cl->count, NULL, cl->log_n, sms, lift);
+		} else if (cl->fused) {
 			e = vkcu_polymul_lift(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, sms, lift);
 		} else {
 			const vkcu_ntt_job *nj = dev_ntt + 3 * (size_t) cl->first;
@@ -226,14 +261,22 @@ int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, cons
 	return 0;
 }
 
-/* Fill the three ntt-job arrays of every composed class from the poly jobs. */
+/* Fill the ntt-job arrays from the recorded jobs: three per job of a composed
+ * polymul class, one per job of a transform class. */
 void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struct vkh_job_class *classes,
 		uint32_t nclasses) {
 	for (uint32_t k = 0; k < nclasses; k++) {
 		const struct vkh_job_class *cl = &classes[k];
+		vkcu_ntt_job *nj = ntt + 3 * (size_t) cl->first;
+		if (cl->kind != VKH_JOB_POLYMUL) { /* one transform job each: in -> out */
+			for (uint32_t i = 0; i < cl->count; i++) {
+				const vkcu_poly_job *j = &poly[cl->first + i];
+				nj[i] = (vkcu_ntt_job){j->a, j->c, j->tw};
+			}
+			continue;
+		}
 		if (cl->fused)
 			continue;
-		vkcu_ntt_job *nj = ntt + 3 * (size_t) cl->first;
 		for (uint32_t i = 0; i < cl->count; i++) {
 			const vkcu_poly_job *j = &poly[cl->first + i];
 			nj[i] = (vkcu_ntt_job){j->b, j->scratch, j->tw};
@@ -288,11 +331,12 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	b->nclasses = 0;
 	for (uint32_t i = 0; i < b->njobs; i++) {
 		struct job_rec *r = &b->recs[i];
-		if (b->nclasses == 0 || b->classes[b->nclasses - 1].log_n != r->log_n ||
-				b->classes[b->nclasses - 1].lift != r->lift) {
+		if (b->nclasses == 0 || b->classes[b->nclasses - 1].kind != r->kind ||
+				b->classes[b->nclasses - 1].log_n != r->log_n || b->classes[b->nclasses - 1].lift != r->lift) {
 			if (b->nclasses == MAX_CLASSES)
 				return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_commit: too many degree classes");
 			struct vkh_job_class *cl = &b->classes[b->nclasses++];
+			cl->kind = r->kind;
 			cl->log_n = r->log_n;
 			cl->lift = r->lift;
 			cl->first = i;

@@ -95,7 +95,9 @@ int vkh_check_mod(struct vkhel_ctx *ctx, const char *op, uint64_t mod);
 int vkh_lift_compile(struct vkhel_ctx *ctx, const struct vkhel_lift_step *steps, uint32_t nsteps, uint64_t q,
 		vkcu_lift *out);
 /* batch.c -- degree classes of a sorted job list, shared with the server */
+enum { VKH_JOB_POLYMUL = 0, VKH_JOB_FORWARD = 1, VKH_JOB_INVERSE = 2 };
 struct vkh_job_class {
+	uint32_t kind;         /* VKH_JOB_*; transform jobs keep in / out / tables in a, c, tw */
 	uint32_t log_n;
 	uint32_t first, count;
 	int fused;

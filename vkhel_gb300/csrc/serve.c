@@ -179,6 +179,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 			sl->host_poly[i] = tmp[keys[i] & 0xffffffffffull];
 			if (nclasses == 0 || classes[nclasses - 1].log_n != log_n) {
 				struct vkh_job_class *cl = &classes[nclasses++];
+				cl->kind = VKH_JOB_POLYMUL;
 				cl->log_n = log_n;
 				cl->lift = 0;
 				cl->first = i;
