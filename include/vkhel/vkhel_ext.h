@@ -155,7 +155,8 @@ int vkhel_vector_polymul_noalloc(const struct vkhel_vector *a,
  * captured in a CUDA graph), then launched any number of times.  Jobs of
  * different degrees may be mixed; each degree class runs in its own kernel
  * inside the same graph.  Operand memory is read at launch time, so new data
- * in the same vectors is picked up by every launch. */
+ * in the same vectors is picked up by every launch; the vectors must outlive
+ * the batch (it keeps their device addresses, not references). */
 struct vkhel_batch;
 enum vkhel_batch_flags {
 	VKHEL_BATCH_GRAPH = 1   /* capture and replay a CUDA graph */

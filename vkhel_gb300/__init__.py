@@ -432,7 +432,7 @@ class Batch:
 
     def add_polymul(self, tables, a, b, c, lift=None):
         arr = (vp * len(tables))(*[t.ptr for t in tables])
-        self._keep.append(tables)
+        self._keep.append((tables, a, b, c))  # the batch reads and writes them at every launch
         if lift:
             steps, n = lift_steps(lift)
             code = lib().vkhel_batch_add_polymul_lift(self.ptr, arr, len(tables), a.ptr, b.ptr, c.ptr,
