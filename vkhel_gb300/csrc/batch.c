@@ -412,11 +412,9 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 				e = ie;
 			b->graph = exec;
 		}
-	} else {
-		e = issue(b); /* one eager run also validates the launches */
-		if (!e)
-			e = vkcu_sync(ctx->stream);
 	}
+	/* eager batches run nothing here (a job may work in place, so a trial run
+	 * would change its data); their first launch counts the kernels */
 	b->kernels = (uint32_t) (vkcu_launch_count() - before);
 	if (flags & VKHEL_BATCH_GRAPH)
 		vkcu_count_launches((uint64_t) 0 - b->kernels); /* capture executes nothing */
@@ -437,7 +435,10 @@ int vkhel_batch_launch(struct vkhel_batch *b) {
 		if (!e)
 			vkcu_count_launches(b->kernels);
 	} else {
+		const uint64_t before = vkcu_launch_count();
 		e = issue(b);
+		if (!e && !b->kernels)
+			b->kernels = (uint32_t) (vkcu_launch_count() - before);
 	}
 	vkcu_range_pop();
 	return vkh_cuda(b->ctx, e, "batch_launch");
