@@ -198,7 +198,8 @@ int vkhel_batch_launch(struct vkhel_batch *batch);
 /* Launch and wait. */
 int vkhel_batch_run(struct vkhel_batch *batch);
 uint32_t vkhel_batch_jobs(const struct vkhel_batch *batch);
-/* Kernels one launch of the batch issues. */
+/* Kernels one launch of the batch issues (known after commit for a graph
+ * batch, after the first launch otherwise: commit itself runs nothing). */
 uint32_t vkhel_batch_kernels(const struct vkhel_batch *batch);
 void vkhel_batch_destroy(struct vkhel_batch *batch);
 

@@ -33,11 +33,12 @@ def test_rns_batch(vk, ctx, oracle, graph):
         vc = vk.Vector(ctx, limbs * n)
         batch.add_polymul(tabs, va, vb, vc)
         vecs.append((va, vb, vc))
-    batch.commit(graph=graph)
-    assert batch.jobs == pairs * limbs and batch.kernels >= 1
+    batch.commit(graph=graph)  # runs nothing
+    assert batch.jobs == pairs * limbs
+    assert all(not vc.download().any() for _, _, vc in vecs)
     before = vk.launch_count()
     batch.run()
-    assert vk.launch_count() - before == batch.kernels
+    assert batch.kernels >= 1 and vk.launch_count() - before == batch.kernels
     for i, (va, vb, vc) in enumerate(vecs):
         _check(oracle, qs, ws, a[i].ravel(), b[i].ravel(), vc.download(), n)
     # new operand data in the same vectors is picked up by the next launch
