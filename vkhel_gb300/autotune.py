@@ -2,11 +2,12 @@
 
     python -m vkhel_gb300.autotune            # writes vkhel_gb300/tuning/gb300.txt (+ _report.json)
 
-For every fused polymul degree 2^8 .. 2^14 it times each compiled variant
-(words per thread, radix-16 groups in flight per thread) on a batch that
-fills the GPU several times over (one limb product per job, a 60-bit prime,
-uniform operands), and for ragged batches it times running the degree
-classes sequentially against running them on concurrent streams.  The
+For every CTA-resident degree 2^8 .. 2^14 it times each compiled variant
+(words per thread, radix-16 groups in flight per thread) of the fused
+polymul, the forward and the inverse transform on a batch that fills the GPU
+several times over (one limb job per polynomial, a 60-bit prime, uniform
+operands), and for ragged batches it times running the degree classes
+sequentially against running them on concurrent streams.  The
 fastest choice of each is written to the table libvkhel reads at start-up
 (see vkhel_tune_* in include/vkhel/vkhel_ext.h).  Every variant computes the
 same words (tests/test_gpu_variants.py checks them against the oracle), so
@@ -80,6 +81,32 @@ def tune_polymul(ctx, sms, reps=10):
     return best, report
 
 
+def tune_transforms(ctx, sms, family, reps=10):
+    """Variants of the forward (family 1) or inverse (family 2) transform."""
+    L = vk.lib()
+    best, report = {}, {}
+    for log_n, variants in VARIANTS.items():
+        n = 1 << log_n
+        count = 4 * sms * max(1, (1 << 14) // n)
+        t, a, b, c = _single_limb_jobs(ctx, log_n, count, seed=100 + log_n)
+        times = {}
+        for v in variants:
+            L.vkhel_tune_set(family, log_n, v)
+            bt = vk.Batch(ctx)
+            bt.add_transform([t] * count, a, c, inverse=family == INVERSE)
+            bt.commit(graph=False)  # the variant is read at every launch
+            times[v] = _time_batch(ctx, bt, reps)
+            bt.close()
+        v_best = min(times, key=times.get)
+        L.vkhel_tune_set(family, log_n, v_best)
+        best[log_n] = v_best
+        report[str(log_n)] = {"jobs": count, "seconds_per_batch": {str(k): x for k, x in times.items()},
+                              "chosen": v_best, "chosen_is": DESCRIBE[v_best]}
+        for x in (a, b, c):
+            x.close()
+    return best, report
+
+
 def tune_concurrency(ctx, reps=5, instances=256):
     L = vk.lib()
     inst = workloads.ragged_instances(instances, seed=33)
@@ -117,20 +144,27 @@ def main(argv):
     ctx = vk.Context()
     sms = ctx.sm_count
     best, report = tune_polymul(ctx, sms)
+    fwd, fwd_report = tune_transforms(ctx, sms, FORWARD)
+    inv, inv_report = tune_transforms(ctx, sms, INVERSE)
     conc, conc_report = tune_concurrency(ctx)
     ctx.close()
     os.makedirs(os.path.dirname(out_table), exist_ok=True)
     lines = ["# vkhel kernel variants for NVIDIA GB300 (sm_103a), written by `python -m vkhel_gb300.autotune`",
-             "# family log_n variant   (family 0 = fused polymul; family 3 log_n 0 = concurrent degree classes)"]
+             "# family log_n variant   (family 0 = fused polymul, 1 = forward, 2 = inverse;",
+             "#                         family 3 log_n 0 = concurrent degree classes)"]
     lines += [f"{POLYMUL} {log_n} {v}" for log_n, v in sorted(best.items())]
+    lines += [f"{FORWARD} {log_n} {v}" for log_n, v in sorted(fwd.items())]
+    lines += [f"{INVERSE} {log_n} {v}" for log_n, v in sorted(inv.items())]
     lines += [f"{BATCH} 0 {conc}"]
     with open(out_table, "w") as f:
         f.write("\n".join(lines) + "\n")
-    rep = {"gpu_sms": sms, "polymul": report, "batch_classes": conc_report,
+    rep = {"gpu_sms": sms, "polymul": report, "forward": fwd_report, "inverse": inv_report,
+           "batch_classes": conc_report,
            "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     with open(os.path.splitext(out_table)[0] + "_report.json", "w") as f:
         json.dump(rep, f, indent=1)
-    print(json.dumps({"table": out_table, "polymul": best, "concurrent_classes": conc}))
+    print(json.dumps({"table": out_table, "polymul": best, "forward": fwd, "inverse": inv,
+                      "concurrent_classes": conc}))
 
 
 if __name__ == "__main__":
