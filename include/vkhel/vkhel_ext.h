@@ -97,7 +97,9 @@ void vkhel_vector_elemfma_canonical(const struct vkhel_vector *a,
 		uint64_t multiplier, uint64_t mod);
 /* Negacyclic product result = a * b mod (X^n + 1, q) of the first n words,
  * equal to the reference composition forward(a), forward(b), elemmul,
- * inverse.  One fused launch for 256 <= n <= 16384.  Returns a status. */
+ * inverse.  One fused launch for 256 <= n <= 131072 (one CTA, or a cluster
+ * of CTAs sharing the polynomial through distributed shared memory).
+ * Returns a status. */
 int vkhel_vector_polymul(const struct vkhel_vector *a,
 		const struct vkhel_vector *b, struct vkhel_vector *result,
 		struct vkhel_ntt_tables *ntt);
