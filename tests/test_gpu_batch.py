@@ -144,3 +144,26 @@ def test_batch_transform_rejects_bad_arguments(vk, ctx):
         bt.add_transform([t], x, y)                                          # output too short
     with pytest.raises(vk.VkhelError):
         bt.add_transform([t], x, x, inverse=False, lift=[("elemmod", 3, 0)])  # lift on a forward
+
+
+@pytest.mark.parametrize("log_n", [6, 10, 14, 15, 17])
+def test_polymul_result_may_alias_the_second_operand(vk, ctx, oracle, log_n):
+    """c = b (the fused kernels park NTT(b) in c): single call and batch."""
+    n = 1 << log_n
+    q = workloads.ntt_primes(n, 1)[0]
+    w = workloads.root_for(n, q)
+    t = vk.NttTables(n, q, w)
+    rng = np.random.default_rng(log_n + 300)
+    a_h, b_h = workloads.uniform(rng, q, n), workloads.uniform(rng, q, n)
+    ref, _ = oracle.polymul(a_h, b_h, n, q, w)
+    a, b = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h)
+    vk.polymul(a, b, b, t)
+    np.testing.assert_array_equal(b.download(), ref, err_msg="single call")
+    jobs = 24  # enough jobs that the batch takes the one-CTA / cluster-per-job paths
+    a2 = vk.Vector(ctx, np.tile(a_h, jobs))
+    b2 = vk.Vector(ctx, np.tile(b_h, jobs))
+    bt = vk.Batch(ctx)
+    bt.add_polymul([t] * jobs, a2, b2, b2)
+    bt.commit(graph=True)
+    bt.run()
+    np.testing.assert_array_equal(b2.download(), np.tile(ref, jobs), err_msg="batch")
