@@ -10,9 +10,9 @@
 //   elemmodbytwo   src/kernels/shaders/elemmodbytwo.comp:19-27
 // plus elemfma_canonical, the exact (a m + b) mod q.
 //
-// These are HBM-bound streams: each thread moves two words per operand with
-// 16-byte vector accesses, the grid is a multiple of the SM count and loops
-// grid-stride; one scalar tail element is handled by the last thread.
+// These are HBM-bound streams: each thread moves groups of 16-byte pairs
+// (loads first), the grid is at most 8 CTAs per SM and loops grid-stride;
+// one scalar tail element is handled by one thread.
 #include <cuda_runtime.h>
 
 #include "elem_ops.cuh"
@@ -20,25 +20,53 @@
 
 namespace vk {
 
-// B == nullptr for unary operations.
-template <class Op>
+// B == nullptr for unary operations.  Each thread moves P 16-byte pairs of
+// every operand per iteration (2 for binary ops, 4 for unary ones, so both
+// keep about the same bytes in flight), all loads issued before the first
+// store; lanes past the end re-read the last pair and store nothing.
+template <class Op, bool BIN>
 __global__ void __launch_bounds__(256) k_elementwise(u64* __restrict__ res, const u64* a, const u64* b, u64 len,
                                                      Op op) {
+  constexpr int P = BIN ? 2 : 4;
   const u64 pairs = len >> 1;
-  const u64 stride = (u64)gridDim.x * blockDim.x;
-  for (u64 p = (u64)blockIdx.x * blockDim.x + threadIdx.x; p < pairs; p += stride) {
-    const ulonglong2 x = ld2(a + 2 * p);
-    ulonglong2 y = make_ulonglong2(0, 0);
-    if (b) y = ld2(b + 2 * p);
-    st2(res + 2 * p, op(x.x, y.x), op(x.y, y.y));
+  const u64 step = (u64)gridDim.x * blockDim.x * P;
+  for (u64 g0 = (u64)blockIdx.x * blockDim.x * P; g0 < pairs; g0 += step) {
+    ulonglong2 x[P], y[BIN ? P : 1];
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+      const u64 p = g0 + threadIdx.x + (u64)k * blockDim.x;
+      const u64 pc = p < pairs ? p : pairs - 1;
+      x[k] = ld2(a + 2 * pc);
+      if constexpr (BIN) y[k] = ld2(b + 2 * pc);
+    }
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+      const u64 p = g0 + threadIdx.x + (u64)k * blockDim.x;
+      const ulonglong2 yk = BIN ? y[BIN ? k : 0] : make_ulonglong2(0, 0);
+      if (p < pairs) st2(res + 2 * p, op(x[k].x, yk.x), op(x[k].y, yk.y));
+    }
   }
   if ((len & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
     const u64 i = len - 1;
-    res[i] = op(a[i], b ? b[i] : 0ull);
+    res[i] = op(a[i], BIN ? b[i] : 0ull);
   }
 }
 
 static int g_sms = 0;
+
+// One wave of resident blocks (the kernel's occupancy, looked up once per
+// instantiation), or fewer when there is less work.
+template <auto kernel>
+static unsigned grid(u64 want) {
+  static const int per_sm = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0) != cudaSuccess || b < 1) b = 1;
+    return b;
+  }();
+  const u64 cap = (u64)g_sms * per_sm;
+  const u64 n = want < cap ? want : cap;
+  return (unsigned)(n ? n : 1);
+}
 
 template <class Op>
 static int launch(void* stream, uint64_t* res, const uint64_t* a, const uint64_t* b, uint64_t len, Op op) {
@@ -51,12 +79,15 @@ static int launch(void* stream, uint64_t* res, const uint64_t* a, const uint64_t
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_sms <= 0) g_sms = 1;
   }
-  const u64 pairs = (len + 1) / 2;
-  u64 blocks = (pairs + 255) / 256;
-  const u64 cap = (u64)g_sms * 8;
-  if (blocks > cap) blocks = cap;
-  k_elementwise<Op><<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
-      reinterpret_cast<u64*>(res), reinterpret_cast<const u64*>(a), reinterpret_cast<const u64*>(b), len, op);
+  const u64 per_block = 256 * (b ? 2 : 4);  // pairs a block moves per iteration
+  const u64 want = ((len + 1) / 2 + per_block - 1) / per_block;
+  auto* r = reinterpret_cast<u64*>(res);
+  auto* x = reinterpret_cast<const u64*>(a);
+  auto* y = reinterpret_cast<const u64*>(b);
+  if (b)
+    k_elementwise<Op, true><<<grid<k_elementwise<Op, true>>(want), 256, 0, (cudaStream_t)stream>>>(r, x, y, len, op);
+  else
+    k_elementwise<Op, false><<<grid<k_elementwise<Op, false>>(want), 256, 0, (cudaStream_t)stream>>>(r, x, y, len, op);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
 }
