@@ -75,16 +75,17 @@ def test_batch_commit_failure_then_fresh_batch(vk, ctx, oracle):
     np.testing.assert_array_equal(c.download(), oracle.polymul(a_h, b_h, n, q, w)[0])
 
 
-def test_table_upload_failure_then_success(vk, ctx, oracle):
+def test_table_upload_failure_then_success(vk, oracle):
     n = 1 << 10
     q, w, a_h, _ = _operands(n, 2)
     t = vk.NttTables(n, q, w)
-    a, r = vk.Vector(ctx, a_h), vk.Vector(ctx, n)
-    vk.fail_allocations(0, 1)           # the context's first use of (n, q, w): its device tables
-    with pytest.raises(vk.VkhelError):
+    with vk.Context() as fresh:         # no tables resident yet
+        a, r = vk.Vector(fresh, a_h), vk.Vector(fresh, n)
+        vk.fail_allocations(0, 1)       # the context's first use of (n, q, w): its device tables
+        with pytest.raises(vk.VkhelError):
+            vk.forward_transform(a, r, t)
         vk.forward_transform(a, r, t)
-    vk.forward_transform(a, r, t)
-    np.testing.assert_array_equal(r.download(), oracle.forward(a_h, n, q, w)[0])
+        np.testing.assert_array_equal(r.download(), oracle.forward(a_h, n, q, w)[0])
 
 
 def test_budget_exhaustion(vk, ctx):
