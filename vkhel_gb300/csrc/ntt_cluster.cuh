@@ -1,3 +1,4 @@
+#pragma once
 // Transforms and fused polynomial multiply for n = 2^15 .. 2^17 on a thread-
 // block cluster of C = n / 2^14 CTAs with distributed shared memory (the
 // four-step decomposition):
@@ -276,36 +277,12 @@ using Small13 = Shape<13, 32>;
     default: return (int)cudaErrorInvalidValue;              \
   }
 
-int fwd_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs) {
-#define X(L, S) launch_cluster<L, S, k_ntt_fwd_cluster<L, S>>(st, njobs, jobs, njobs, one)
-  VK_CLUSTER_SHAPES(X)
-#undef X
-}
-
-int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs,
-                const vkcu_lift* lift) {
-  const vkcu_lift l = lift ? *lift : vkcu_lift{};
-  if (lift) {
-#define X(L, S) launch_cluster<L, S, k_ntt_inv_cluster<L, S, true>>(st, njobs, jobs, njobs, one, l)
-    VK_CLUSTER_SHAPES(X)
-#undef X
-  }
-#define X(L, S) launch_cluster<L, S, k_ntt_inv_cluster<L, S, false>>(st, njobs, jobs, njobs, one, l)
-  VK_CLUSTER_SHAPES(X)
-#undef X
-}
-
-int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc, int logs,
-                 const vkcu_lift* lift) {
-  const vkcu_lift l = lift ? *lift : vkcu_lift{};
-  if (lift) {
-#define X(L, S) launch_cluster<L, S, k_polymul_cluster<L, S, true>>(st, njobs, jobs, njobs, one, l)
-    VK_CLUSTER_SHAPES(X)
-#undef X
-  }
-#define X(L, S) launch_cluster<L, S, k_polymul_cluster<L, S, false>>(st, njobs, jobs, njobs, one, l)
-  VK_CLUSTER_SHAPES(X)
-#undef X
-}
+// The lifted inverse and polymul kernels are instantiated in their own
+// translation units (ntt_cluster_inv_lift.cu, ntt_cluster_poly_lift.cu) so
+// that the cluster kernels compile in parallel.
+int inv_cluster_lifted(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,
+                       int logs, const vkcu_lift& lift);
+int poly_cluster_lifted(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
+                        int logs, const vkcu_lift& lift);
 
 }  // namespace vk

@@ -1,0 +1,15 @@
+// Inverse transform on a thread-block cluster (the kernels are in ntt_cluster.cuh).
+#include "ntt_cluster.cuh"
+
+namespace vk {
+
+int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc, int logs,
+                const vkcu_lift* lift) {
+  if (lift) return inv_cluster_lifted(st, jobs, njobs, one, logc, logs, *lift);
+  const vkcu_lift l{};
+#define X(L, S) launch_cluster<L, S, k_ntt_inv_cluster<L, S, false>>(st, njobs, jobs, njobs, one, l)
+  VK_CLUSTER_SHAPES(X)
+#undef X
+}
+
+}  // namespace vk
