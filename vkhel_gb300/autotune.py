@@ -55,7 +55,7 @@ def _single_limb_jobs(ctx, log_n, count, seed):
     return t, a, b, c
 
 
-def tune_polymul(ctx, sms, reps=10):
+def tune_polymul(ctx, sms, reps=30):
     L = vk.lib()
     best, report = {}, {}
     for log_n, variants in VARIANTS.items():
@@ -81,7 +81,7 @@ def tune_polymul(ctx, sms, reps=10):
     return best, report
 
 
-def tune_transforms(ctx, sms, family, reps=10):
+def tune_transforms(ctx, sms, family, reps=30):
     """Variants of the forward (family 1) or inverse (family 2) transform."""
     L = vk.lib()
     best, report = {}, {}

@@ -198,8 +198,11 @@ __global__ void __launch_bounds__(S::T, 1)
           u64 bh[16];
           load16(bh, scratch + 16 * g);
 #pragma unroll
-          for (int j = 0; j < 16; j++)
-            sm[pad(16 * g + j)] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+          for (int j = 0; j < 16; j++) v[j] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+          // the sub-block's first inverse pass (stages HEAD + 3 .. HEAD) on the same words
+          gs_group<4, 0, false, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+#pragma unroll
+          for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
         }
       });
     }
@@ -207,7 +210,7 @@ __global__ void __launch_bounds__(S::T, 1)
       const vkcu_poly_job nx = fetch_job(jobs, one, w + ncl);
       prefetch_l2(reinterpret_cast<const u64*>(nx.b) + (size_t)threadIdx.x * K::SUB + rank * K::COLS, kSlice);
     }
-    inv_passes<S>(sm, t, tw_mult, S::HEAD);
+    inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
     inv_last_smem<S>(sm, t, tw_mult);
     cl.sync();
     col_inv_out<LOGC, S, LIFT>(reinterpret_cast<u64*>(job.c), sm, cl, rank, t, &lift);

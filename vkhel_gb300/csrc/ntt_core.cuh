@@ -523,7 +523,8 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
 // Fused c = INTT(NTT(a) . NTT(b)).  Phase 0 transforms b and parks NTT(b)
 // (canonical) in job.scratch; phase 1 transforms a with the same code, and its
 // last pass multiplies by NTT(b) (read back at the words this thread wrote)
-// into shared memory; the inverse transform then writes c.  a is prefetched
+// and runs the first inverse pass on the products in the same registers; the
+// rest of the inverse transform then writes c.  a is prefetched
 // into L2 while b is transformed, the next job's b while a is.
 template <int LOGN, int E, int U, bool LIFT = false>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
@@ -554,12 +555,15 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
           u64 bh[16];
           load16(bh, scratch + 16 * g);
 #pragma unroll
-          for (int j = 0; j < 16; j++)
-            sm[pad(16 * g + j)] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+          for (int j = 0; j < 16; j++) v[j] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+          // the first inverse pass (stages HEAD + 3 .. HEAD) on the same 16 words
+          gs_group<4, 0, false, false>(v, t.inv, (1u << S::HEAD) + (u32)g, t);
+#pragma unroll
+          for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
         }
       });
     }
-    inv_passes<S>(sm, t, 1u, S::HEAD);
+    inv_passes<S>(sm, t, 1u, S::HEAD - 4);
     inv_last<S, LIFT>(sm, t, 1u, reinterpret_cast<u64*>(job.c), true, &lift);
     __syncthreads();
   }
