@@ -47,52 +47,62 @@ struct Cols {
 };
 
 // Forward column pass: global stages 0 .. LOGC-1 (exact first-stage rule),
-// outputs scattered to the owning CTAs' shared memory, lazy [0, 4q).
+// outputs scattered to the owning CTAs' shared memory, lazy [0, 4q).  A
+// thread's PER columns go in two rounds of H = PER / 2 (16 words in flight:
+// all 32 at once would spill).
 template <int LOGC, class S>
 __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, const cg::cluster_group& cl, int rank,
                                         const Tw& t) {
   using K = Cols<LOGC, S>;
-  u64 v[K::PER * K::C];
-#pragma unroll
-  for (int k = 0; k < K::PER; k++)
-#pragma unroll
-    for (int j = 0; j < K::C; j++) v[k * K::C + j] = ld_stream(in + K::col(rank, k) + (size_t)j * K::SUB);
+  constexpr int H = K::PER >= 2 ? K::PER / 2 : 1;
   const ulonglong2 w0 = ld_tw(t.fwd + 1);
-  static_for<0, K::PER>([&](auto kc) {
-    constexpr int k = decltype(kc)::value;
+#pragma unroll 1
+  for (int k0 = 0; k0 < K::PER; k0 += H) {
+    u64 v[H * K::C];
 #pragma unroll
-    for (int jj = 0; jj < K::C / 2; jj++) ct_first(v[k * K::C + jj], v[k * K::C + jj + K::C / 2], w0.x, w0.y, t);
-    ct_group<LOGC, 1, k * K::C>(v, t.fwd, 1u, t);
-  });
+    for (int k = 0; k < H; k++)
 #pragma unroll
-  for (int j = 0; j < K::C; j++) {
-    u64* rem = cl.map_shared_rank(sm, j);
+      for (int j = 0; j < K::C; j++) v[k * K::C + j] = ld_stream(in + K::col(rank, k0 + k) + (size_t)j * K::SUB);
+    static_for<0, H>([&](auto kc) {
+      constexpr int k = decltype(kc)::value;
 #pragma unroll
-    for (int k = 0; k < K::PER; k++) rem[pad(K::col(rank, k))] = v[k * K::C + j];
+      for (int jj = 0; jj < K::C / 2; jj++) ct_first(v[k * K::C + jj], v[k * K::C + jj + K::C / 2], w0.x, w0.y, t);
+      ct_group<LOGC, 1, k * K::C>(v, t.fwd, 1u, t);
+    });
+#pragma unroll
+    for (int j = 0; j < K::C; j++) {
+      u64* rem = cl.map_shared_rank(sm, j);
+#pragma unroll
+      for (int k = 0; k < H; k++) rem[pad(K::col(rank, k0 + k))] = v[k * K::C + j];
+    }
   }
 }
 
 // Inverse column pass: gather, global stages LOGC-1 .. 0 with n^-1 folded in,
-// canonical words to global memory.
+// canonical words to global memory; two rounds of H columns as above.
 template <int LOGC, class S, class Epi>
 __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
                                         const Tw& t, const Epi& epi) {
   using K = Cols<LOGC, S>;
-  u64 v[K::PER * K::C];
+  constexpr int H = K::PER >= 2 ? K::PER / 2 : 1;
+#pragma unroll 1
+  for (int k0 = 0; k0 < K::PER; k0 += H) {
+    u64 v[H * K::C];
 #pragma unroll
-  for (int j = 0; j < K::C; j++) {
-    const u64* rem = cl.map_shared_rank(sm, j);
+    for (int j = 0; j < K::C; j++) {
+      const u64* rem = cl.map_shared_rank(sm, j);
 #pragma unroll
-    for (int k = 0; k < K::PER; k++) v[k * K::C + j] = rem[pad(K::col(rank, k))];
+      for (int k = 0; k < H; k++) v[k * K::C + j] = rem[pad(K::col(rank, k0 + k))];
+    }
+    static_for<0, H>([&](auto kc) {
+      constexpr int k = decltype(kc)::value;
+      gs_group<LOGC, k * K::C, false, true>(v, t.inv, 1u, t);
+    });
+#pragma unroll
+    for (int k = 0; k < H; k++)
+#pragma unroll
+      for (int j = 0; j < K::C; j++) out[K::col(rank, k0 + k) + (size_t)j * K::SUB] = epi(v[k * K::C + j]);
   }
-  static_for<0, K::PER>([&](auto kc) {
-    constexpr int k = decltype(kc)::value;
-    gs_group<LOGC, k * K::C, false, true>(v, t.inv, 1u, t);
-  });
-#pragma unroll
-  for (int k = 0; k < K::PER; k++)
-#pragma unroll
-    for (int j = 0; j < K::C; j++) out[K::col(rank, k) + (size_t)j * K::SUB] = epi(v[k * K::C + j]);
 }
 
 template <int LOGC, class S, bool LIFT>
