@@ -249,29 +249,35 @@ struct Pass16 {
   __device__ __forceinline__ u32 base(int g) const { return tw0 + (u32)(g >> lt); }
 };
 
-// First forward pass: all of this thread's words come from global memory at
-// once (coalesced), then FIRSTK stages per group, results to shared memory.
+// First forward pass: this thread's words come from global memory (coalesced)
+// in rounds of 16 (all of a round's loads in flight at once; 32 words at once
+// would spill), then FIRSTK stages per group, results to shared memory.
 // The first sub-stage uses the exact first-stage rule; after the global pass
 // of a large transform the inputs are < 2q and always take its fast path.
 template <class S>
 __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, const Tw& t, u32 tw_mult) {
   constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
-  u64 v[S::E];
+  constexpr int GR = (16 >> KK) < 1 ? 1 : (G < (16 >> KK) ? G : (16 >> KK));  // groups per round
+#pragma unroll 1
+  for (int i0 = 0; i0 < G; i0 += GR) {
+    u64 v[GR << KK];
 #pragma unroll
-  for (int i = 0; i < G; i++)
+    for (int i = 0; i < GR; i++)
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[i * (1 << KK) + j] = ld_stream(in + (int)threadIdx.x + i * S::T + j * TMIN);
-  const ulonglong2 w0 = ld_tw(t.fwd + tw_mult);
-  static_for<0, G>([&](auto ic) {
-    constexpr int i = decltype(ic)::value;
+      for (int j = 0; j < (1 << KK); j++)
+        v[i * (1 << KK) + j] = ld_stream(in + (int)threadIdx.x + (i0 + i) * S::T + j * TMIN);
+    const ulonglong2 w0 = ld_tw(t.fwd + tw_mult);
+    static_for<0, GR>([&](auto ic) {
+      constexpr int i = decltype(ic)::value;
 #pragma unroll
-    for (int jj = 0; jj < (1 << (KK - 1)); jj++)
-      ct_first(v[i * (1 << KK) + jj], v[i * (1 << KK) + jj + (1 << (KK - 1))], w0.x, w0.y, t);
-    ct_group<KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
-    const int g = (int)threadIdx.x + i * S::T;
+      for (int jj = 0; jj < (1 << (KK - 1)); jj++)
+        ct_first(v[i * (1 << KK) + jj], v[i * (1 << KK) + jj + (1 << (KK - 1))], w0.x, w0.y, t);
+      ct_group<KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
+      const int g = (int)threadIdx.x + (i0 + i) * S::T;
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
-  });
+      for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
+    });
+  }
   __syncthreads();
 }
 
