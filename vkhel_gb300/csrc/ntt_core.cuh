@@ -249,6 +249,14 @@ struct Pass16 {
   __device__ __forceinline__ u32 base(int g) const { return tw0 + (u32)(g >> lt); }
 };
 
+// Groups of 2^KK words a thread handles at once in the passes that walk G
+// such groups: 16 words per round (fewer leave too little independent work
+// between the loads and the stores of a round; more spill).
+template <int KK, int G>
+constexpr int round_groups() {
+  return (16 >> KK) < 1 ? 1 : (G < (16 >> KK) ? G : (16 >> KK));
+}
+
 // First forward pass: this thread's words come from global memory (coalesced)
 // in rounds of 16 (all of a round's loads in flight at once; 32 words at once
 // would spill), then FIRSTK stages per group, results to shared memory.
@@ -257,7 +265,7 @@ struct Pass16 {
 template <class S>
 __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, const Tw& t, u32 tw_mult) {
   constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
-  constexpr int GR = (16 >> KK) < 1 ? 1 : (G < (16 >> KK) ? G : (16 >> KK));  // groups per round
+  constexpr int GR = round_groups<KK, G>();
 #pragma unroll 1
   for (int i0 = 0; i0 < G; i0 += GR) {
     u64 v[GR << KK];
@@ -285,16 +293,20 @@ __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, c
 // cluster transform): groups of 2^FIRSTK words, twiddle base tw_mult.
 template <class S>
 __device__ __forceinline__ void fwd_first_smem(u64* sm, const Tw& t, u32 tw_mult) {
-  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK, GR = round_groups<KK, G>();
 #pragma unroll 1
-  for (int i = 0; i < G; i++) {
-    const int g = (int)threadIdx.x + i * S::T;
-    u64 v[1 << KK];
+  for (int i0 = 0; i0 < G; i0 += GR) {
+    const int g0 = (int)threadIdx.x + i0 * S::T;
+    u64 v[GR << KK];
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];
-    ct_group<KK, 0, 0>(v, t.fwd, tw_mult, t);
+    for (int i = 0; i < GR; i++)
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[j];
+      for (int j = 0; j < (1 << KK); j++) v[i * (1 << KK) + j] = sm[pad(g0 + i * S::T + j * TMIN)];
+    static_for<0, GR>([&](auto ic) { ct_group<KK, 0, decltype(ic)::value * (1 << KK)>(v, t.fwd, tw_mult, t); });
+#pragma unroll
+    for (int i = 0; i < GR; i++)
+#pragma unroll
+      for (int j = 0; j < (1 << KK); j++) sm[pad(g0 + i * S::T + j * TMIN)] = v[i * (1 << KK) + j];
   }
   __syncthreads();
 }
@@ -354,23 +366,25 @@ __device__ __forceinline__ void inv_passes(u64* sm, const Tw& t, u32 tw_mult, in
 // shared memory, lazy [0, 2q), followed by a barrier.
 template <class S>
 __device__ __forceinline__ void inv_last_smem(u64* sm, const Tw& t, u32 tw_mult) {
-  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
+  constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK, GR = round_groups<KK, G>();
 #pragma unroll 1
-  for (int i = 0; i < G; i++) {
-    const int g = (int)threadIdx.x + i * S::T;
-    u64 v[1 << KK];
+  for (int i0 = 0; i0 < G; i0 += GR) {
+    const int g0 = (int)threadIdx.x + i0 * S::T;
+    u64 v[GR << KK];
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];
-    gs_group<KK, 0, false, false>(v, t.inv, tw_mult, t);
+    for (int i = 0; i < GR; i++)
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[j];
+      for (int j = 0; j < (1 << KK); j++) v[i * (1 << KK) + j] = sm[pad(g0 + i * S::T + j * TMIN)];
+    static_for<0, GR>(
+        [&](auto ic) { gs_group<KK, decltype(ic)::value * (1 << KK), false, false>(v, t.inv, tw_mult, t); });
+#pragma unroll
+    for (int i = 0; i < GR; i++)
+#pragma unroll
+      for (int j = 0; j < (1 << KK); j++) sm[pad(g0 + i * S::T + j * TMIN)] = v[i * (1 << KK) + j];
   }
   __syncthreads();
 }
 
-// Last inverse pass (stages FIRSTK-1 .. 0) from shared memory to `out`,
-// coalesced.  fold: whole transform, n^-1 folded into stage 0, canonical
-// output; otherwise lazy [0, 2q).
 // Epilogue of the inverse transforms: the reference's centred-lift ops in
 // order on each canonical output word (src/vector.c:342-386, 429-511), with
 // the job's modulus resolved once per job for VKCU_LIFT_TABLE_Q steps.
@@ -408,6 +422,10 @@ struct NoLift {
   __device__ __forceinline__ u64 operator()(u64 x) const { return x; }
 };
 
+// Last inverse pass (stages FIRSTK-1 .. 0) from shared memory to `out`,
+// coalesced, one group at a time (rounds of 16 words measured slower here).
+// fold: whole transform, n^-1 folded into stage 0, canonical output;
+// otherwise lazy [0, 2q).
 template <class S, class Epi>
 __device__ __forceinline__ void inv_last_epi(u64* sm, const Tw& t, u32 tw_mult, u64* __restrict__ out, bool fold,
                                              const Epi& epi) {
