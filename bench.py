@@ -32,6 +32,7 @@ Under torchrun each rank runs an independent replica (no collective on the
 data path); value and e2e are summed over ranks with the max time.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -70,44 +71,56 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi sampling (every 50 ms) during the timed region."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
+        self.window = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+
+    def mark(self, t0, t1):
+        """Wall-clock bounds (time.time()) of the timed region."""
+        self.window = (t0, t1)
 
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
-        sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         for line in out.splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                ts = None
+            try:
+                rows.append((ts, float(f[2]), float(f[3]), {nm for nm, v in zip(names, f[6:10]) if v.lower() == "active"}))
             except ValueError:
                 continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "samples": len(sm),
-                "reasons": sorted(reasons)}
+        inside = rows
+        if self.window:
+            t0, t1 = self.window
+            inside = [r for r in rows if r[0] is not None and t0 - 0.025 <= r[0] <= t1 + 0.025] or rows
+        sm = [r[1] for r in inside]
+        reasons = set().union(*[r[3] for r in inside]) if inside else set()
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": inside[-1][2] if inside else None,
+                "samples": len(sm), "samples_in_timed_region": len(inside) if inside is not rows else 0,
+                "interval_ms": 50, "reasons": sorted(reasons)}
 
 
 def reference_arm(args, rank, world):
@@ -577,7 +590,7 @@ EXTRAS = {"single_limb_batch": single_limb_batch, "ragged_batch": ragged_batch,
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -674,6 +687,7 @@ def main():
     launches0 = vk.launch_count()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = [torch.cuda.Event(enable_timing=True) for _ in ctxs]
+    wall0 = time.time()
     t_start.record(streams[0])
     streams[1].wait_event(t_start)
     for k in range(args.steps):
@@ -682,6 +696,7 @@ def main():
         e.record(st)
     for e in t_end:
         e.synchronize()
+    clocks.mark(wall0, time.time())
     launches = vk.launch_count() - launches0
     total_ms = max(t_start.elapsed_time(e) for e in t_end)
     clk = clocks.stop()
