@@ -76,6 +76,33 @@ def test_mixed_requests_from_threads_match_alone(vk, oracle):
             np.testing.assert_array_equal(alone, c)
 
 
+def test_large_micro_batches_run_in_limb_chunks(vk, oracle):
+    """At low load, micro-batches of at most four requests and 8 MB of
+    operands or more are issued in up to four chunks of limbs (each computing
+    as soon as its operands are up).  First the requests go in small groups,
+    each after the previous group finished: the 12.6 MB request alone runs in
+    three chunks (boundaries inside the request); 6.3 + 3.1 MB, when the
+    scheduler takes the pair together, in two (a boundary between requests).
+    Then all at once, while the first micro-batch runs: the next one takes
+    every queued request that fits and may be chunked too."""
+    rng = np.random.default_rng(41)
+    shapes = [(17, 6), (16, 5), (14, 6), (17, 3), (15, 6), (16, 4)]
+    reqs = [_request(vk, rng, l, k) for l, k in shapes]
+    with vk.Server(max_batch_limbs=20, max_inflight_batches=1) as srv:
+        for pair in ((0,), (1, 2), (3, 4), (5,)):
+            for rid in [srv.submit([t for _, _, t in reqs[i][0]], *reqs[i][1:]) for i in pair]:
+                assert srv.wait(rid) == 0
+        for tq, a, b, c in reqs:
+            _check(oracle, tq, a, b, c)
+            c[:] = 0
+        ids = [srv.submit([t for _, _, t in tq], a, b, c) for tq, a, b, c in reqs]
+        for rid in ids:
+            assert srv.wait(rid) == 0
+        assert srv.stats()["completed"] == 2 * len(reqs)
+    for tq, a, b, c in reqs:
+        _check(oracle, tq, a, b, c)
+
+
 def test_admission_under_a_small_budget(vk, oracle):
     rng = np.random.default_rng(5)
     reqs = [_request(vk, rng, 14, 2) for _ in range(12)]
