@@ -135,12 +135,13 @@ def reference_arm(args, rank, world):
     a = a.reshape(-1, N)[:sample]
     b = b.reshape(-1, N)[:sample]
     pidx = np.arange(sample, dtype=np.uint32) % LIMBS
+    tabs = orc.batch_tables(N, qs, ws)  # built once, as a caller of the reference builds its tables
     for _ in range(args.warmup):
-        _, used = orc.polymul_batch(a, b, N, qs, ws, pidx)
+        _, used = orc.polymul_batch(a, b, N, qs, ws, pidx, tables=tabs)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        _, used = orc.polymul_batch(a, b, N, qs, ws, pidx)
+        _, used = orc.polymul_batch(a, b, N, qs, ws, pidx, tables=tabs)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = sample * args.steps / total
@@ -152,7 +153,8 @@ def reference_arm(args, rank, world):
         "config": {"workload": WORKLOAD, "n": N, "limbs": LIMBS, "pairs": PAIRS,
                    "sample_per_step": f"{sample} of the {PAIRS * LIMBS} limb products"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
-                         "sample": f"{sample} limb-polymuls (n={N}) per step, oracle/oracle.c -O3 OpenMP"},
+                         "sample": f"{sample} limb-polymuls (n={N}) per step, oracle/oracle.c -O3 OpenMP, "
+                                   "tables of the 8 primes built once before the timed steps"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -164,9 +166,10 @@ def cpu_baseline_sample(qs, ws, a, b, budget_s=10.0):
     orc = pyoracle.load()
     aa, bb = a.reshape(-1, N), b.reshape(-1, N)
     pidx = np.tile(np.arange(LIMBS, dtype=np.uint32), PAIRS)
+    tabs = orc.batch_tables(N, qs, ws)  # built once, as a caller of the reference builds its tables
     done, t0 = 0, time.perf_counter()
     while True:
-        _, used = orc.polymul_batch(aa, bb, N, qs, ws, pidx)
+        _, used = orc.polymul_batch(aa, bb, N, qs, ws, pidx, tables=tabs)
         done += aa.shape[0]
         dt = time.perf_counter() - t0
         if dt > budget_s or done >= 8 * aa.shape[0]:
@@ -174,14 +177,14 @@ def cpu_baseline_sample(qs, ws, a, b, budget_s=10.0):
     # the same on one thread, on the first 64 limb products
     one, t1 = 0, time.perf_counter()
     while True:
-        orc.polymul_batch(aa[:64], bb[:64], N, qs, ws, pidx[:64], threads=1)
+        orc.polymul_batch(aa[:64], bb[:64], N, qs, ws, pidx[:64], threads=1, tables=tabs)
         one += 64
         dt1 = time.perf_counter() - t1
         if dt1 > budget_s / 4:
             break
     return {"value": done / dt, "unit": UNIT, "cores": used, "kind": "port",
             "sample": f"{done} limb-polymuls (the {aa.shape[0]}-limb batch x {done // aa.shape[0]}), n={N}, "
-                      f"{dt:.1f} s, oracle/oracle.c -O3, OpenMP over limbs",
+                      f"{dt:.1f} s, oracle/oracle.c -O3, OpenMP over limbs, tables built once",
             "value_1_thread": one / dt1, "sample_1_thread": f"{one} limb-polymuls on one thread, {dt1:.1f} s",
             "cpu_model": cpu_model(), "nproc": os.cpu_count()}
 

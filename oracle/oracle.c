@@ -354,17 +354,10 @@ void orc_negacyclic_schoolbook(const uint64_t *a, const uint64_t *b,
 	}
 }
 
-int orc_polymul_batch(const uint64_t *a, const uint64_t *b, uint64_t *c,
+int orc_polymul_batch_tables(const uint64_t *a, const uint64_t *b, uint64_t *c,
 		size_t count, size_t stride, uint64_t n,
-		const uint64_t *qs, const uint64_t *ws, const uint32_t *prime_idx,
-		size_t n_primes, int threads) {
-	/* One table set per prime, built once like a caller of the reference
-	 * builds one vkhel_ntt_tables per (n, q, w). */
-	uint64_t *tabs = malloc(sizeof(uint64_t) * 4 * n * n_primes);
-	for (size_t p = 0; p < n_primes; p++) {
-		uint64_t *t = tabs + 4 * n * p;
-		orc_ntt_tables(n, qs[p], ws[p], t, t + n, t + 2 * n, t + 3 * n);
-	}
+		const uint64_t *qs, const uint64_t *tabs, const uint32_t *prime_idx,
+		int threads) {
 	int used = 1;
 #ifdef _OPENMP
 	if (threads <= 0)
@@ -390,6 +383,21 @@ int orc_polymul_batch(const uint64_t *a, const uint64_t *b, uint64_t *c,
 		}
 		free(tb);
 	}
+	return used;
+}
+
+int orc_polymul_batch(const uint64_t *a, const uint64_t *b, uint64_t *c,
+		size_t count, size_t stride, uint64_t n,
+		const uint64_t *qs, const uint64_t *ws, const uint32_t *prime_idx,
+		size_t n_primes, int threads) {
+	/* One table set per prime, built once like a caller of the reference
+	 * builds one vkhel_ntt_tables per (n, q, w). */
+	uint64_t *tabs = malloc(sizeof(uint64_t) * 4 * n * n_primes);
+	for (size_t p = 0; p < n_primes; p++) {
+		uint64_t *t = tabs + 4 * n * p;
+		orc_ntt_tables(n, qs[p], ws[p], t, t + n, t + 2 * n, t + 3 * n);
+	}
+	const int used = orc_polymul_batch_tables(a, b, c, count, stride, n, qs, tabs, prime_idx, threads);
 	free(tabs);
 	return used;
 }

@@ -88,6 +88,15 @@ int orc_polymul_batch(const uint64_t *a, const uint64_t *b, uint64_t *c,
 		const uint64_t *qs, const uint64_t *ws, const uint32_t *prime_idx,
 		size_t n_primes, int threads);
 
+/* The same with the primes' tables built beforehand (a caller of the
+ * reference builds one vkhel_ntt_tables per (n, q, w) and reuses it):
+ * tabs = n_primes consecutive sets of the four orc_ntt_tables arrays
+ * (roots, inv_roots, roots_shoup, inv_roots_shoup; 4 n words per prime). */
+int orc_polymul_batch_tables(const uint64_t *a, const uint64_t *b, uint64_t *c,
+		size_t count, size_t stride, uint64_t n,
+		const uint64_t *qs, const uint64_t *tabs, const uint32_t *prime_idx,
+		int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,7 @@ _SIGS = {
     "orc_polymul": (ctypes.c_int, [vp, vp, vp, u64, u64, u64]),
     "orc_negacyclic_schoolbook": (None, [vp, vp, vp, u64, u64]),
     "orc_polymul_batch": (ctypes.c_int, [vp, vp, vp, sz, sz, u64, vp, vp, vp, sz, ctypes.c_int]),
+    "orc_polymul_batch_tables": (ctypes.c_int, [vp, vp, vp, sz, sz, u64, vp, vp, vp, ctypes.c_int]),
 }
 
 
@@ -110,15 +111,29 @@ class Oracle:
         self.L.orc_negacyclic_schoolbook(a.ctypes.data, b.ctypes.data, c.ctypes.data, n, q)
         return c
 
-    def polymul_batch(self, a, b, n, qs, ws, prime_idx, threads=0):
-        """a, b: (count, n) uint64.  Returns (c, threads used)."""
+    def batch_tables(self, n, qs, ws):
+        """The primes' tables for polymul_batch, built once: (len(qs), 4 n) uint64."""
+        t = np.zeros((len(qs), 4 * n), np.uint64)
+        for p, (q, w) in enumerate(zip(qs, ws)):
+            row = t[p]
+            self.L.orc_ntt_tables(n, int(q), int(w), *[row[i * n:].ctypes.data for i in range(4)])
+        return t
+
+    def polymul_batch(self, a, b, n, qs, ws, prime_idx, threads=0, tables=None):
+        """a, b: (count, n) uint64.  Returns (c, threads used).  With `tables`
+        from batch_tables(n, qs, ws) the tables are not rebuilt per call."""
         a, b = _u64(a), _u64(b)
         count = a.shape[0]
         c = np.zeros_like(a)
         qs, ws = _u64(qs), _u64(ws)
         pi = np.ascontiguousarray(np.asarray(prime_idx, dtype=np.uint32))
-        used = self.L.orc_polymul_batch(a.ctypes.data, b.ctypes.data, c.ctypes.data, count, n, n,
-                                        qs.ctypes.data, ws.ctypes.data, pi.ctypes.data, qs.size, threads)
+        if tables is not None:
+            t = np.ascontiguousarray(tables, dtype=np.uint64)
+            used = self.L.orc_polymul_batch_tables(a.ctypes.data, b.ctypes.data, c.ctypes.data, count, n, n,
+                                                   qs.ctypes.data, t.ctypes.data, pi.ctypes.data, threads)
+        else:
+            used = self.L.orc_polymul_batch(a.ctypes.data, b.ctypes.data, c.ctypes.data, count, n, n,
+                                            qs.ctypes.data, ws.ctypes.data, pi.ctypes.data, qs.size, threads)
         return c, used
 
 
