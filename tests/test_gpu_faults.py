@@ -115,6 +115,44 @@ def test_server_fails_only_the_failing_micro_batch(vk, oracle):
         assert srv.stats()["failed"] >= 1
 
 
+def test_server_allocation_failure_after_a_chunk_was_issued(vk, oracle):
+    """A micro-batch pipelined in limb chunks whose second request's buffer
+    cannot be allocated: its first chunk is already uploading and computing.
+    The micro-batch's requests fail with OOM (the first may have completed in
+    a micro-batch of its own, then correctly), its buffers are released only
+    after the issued work, and the server stays usable and exact."""
+    n = 1 << 16
+    qs = workloads.ntt_primes(n, 8)
+    ws = [workloads.root_for(n, q) for q in qs]
+    tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+    rng = np.random.default_rng(12)
+
+    def req(limbs):
+        a = np.concatenate([workloads.uniform(rng, q, n) for q in qs[:limbs]])
+        b = np.concatenate([workloads.uniform(rng, q, n) for q in qs[:limbs]])
+        return tabs[:limbs], a, b, np.zeros(limbs * n, np.uint64)
+
+    def check(r):
+        t, a, b, c = r
+        for k in range(len(t)):
+            s = slice(k * n, (k + 1) * n)
+            np.testing.assert_array_equal(c[s], oracle.polymul(a[s], b[s], n, qs[k], ws[k])[0])
+
+    blocker, first, second, after = req(8), req(6), req(4), req(8)
+    with vk.Server(max_batch_limbs=16, max_inflight_batches=1) as srv:
+        assert srv.wait(srv.submit(*req(8))) == 0        # warm-up: tables resident
+        vk.fail_allocations(2, 1)                          # the blocker's and the first's succeed
+        ids = [srv.submit(*r) for r in (blocker, first, second)]
+        st = [srv.wait(i) for i in ids]
+        assert st[0] == 0 and st[2] == OOM and st[1] in (0, OOM)
+        vk.fail_allocations(0, 0)
+        assert srv.wait(srv.submit(*after)) == 0
+    check(blocker)
+    check(after)
+    if st[1] == 0:
+        check(first)
+
+
 def test_server_cancel_queued_request(vk, oracle):
     n = 1 << 16
     q, w, a_h, b_h = _operands(n, 4)
