@@ -101,3 +101,24 @@ def test_c_extension_program_checks_pass(vk, tmp_path):
     r = subprocess.run([_build_ext(tmp_path)] + _ext_args(), capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 checks failed" in r.stdout
+
+
+# The reference's own programs (test/vector.c, examples/example.c) include
+# only its public header.  Where the reference's sources are present (they
+# are not on GPU machines) they must compile against include/vkhel/vkhel.h
+# and link against libvkhel.so unchanged: the source-level drop-in check.
+REFERENCE_SRC = os.environ.get("VKHEL_REFERENCE_SRC", "/root/reference")
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REFERENCE_SRC, "test", "vector.c")),
+                    reason="the reference's sources are not present on this machine")
+@pytest.mark.parametrize("src", ["test/vector.c", "examples/example.c"])
+def test_reference_programs_compile_and_link_unchanged(vk, tmp_path, src):
+    from vkhel_gb300 import LIB_PATH
+    libdir = os.path.dirname(LIB_PATH)
+    exe = str(tmp_path / os.path.basename(src).replace(".c", ""))
+    r = subprocess.run(["gcc", "-std=gnu11", "-O2", "-I", os.path.join(ROOT, "include", "vkhel"),
+                        os.path.join(REFERENCE_SRC, src), "-o", exe, "-L", libdir, "-lvkhel",
+                        f"-Wl,-rpath,{libdir}", "-Wl,--no-undefined"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "implicit declaration" not in r.stderr, r.stderr
