@@ -526,6 +526,15 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     const Tw t = load_tw(job.tw);
     const u64* in = reinterpret_cast<const u64*>(job.in) + ((size_t)sub << LOGN);
     u64* out = reinterpret_cast<u64*>(job.out) + ((size_t)sub << LOGN);
+    // the next work item's words into L2 while this one runs (2.6-3.4 % on
+    // batched inverse transforms; the forward kernel measured no better so)
+    if (w + (int)gridDim.x < total && threadIdx.x < 4) {
+      const int w2 = w + (int)gridDim.x, sub2 = w2 & ((1 << sub_log) - 1);
+      const vkcu_ntt_job nx = fetch_job(jobs, one, w2 >> sub_log);
+      prefetch_l2(reinterpret_cast<const char*>(reinterpret_cast<const u64*>(nx.in) + ((size_t)sub2 << LOGN)) +
+                      threadIdx.x * (S::N * 2),
+                  S::N * 2);
+    }
     const u32 tw_mult = (1u << sub_log) + sub;
     // first inverse pass (global stage m = n/2 first, exact rule) from global
 #pragma unroll 1
