@@ -26,7 +26,7 @@ enum vkhel_status {
 	VKHEL_ERR_NO_DEVICE = 5,        /* no CUDA device */
 	VKHEL_ERR_TIMEOUT = 6,          /* a bounded wait ran out */
 	VKHEL_ERR_CANCELLED = 7,        /* request cancelled before it ran */
-	VKHEL_ERR_UNSUPPORTED = 8       /* valid request this build does not run */
+	VKHEL_ERR_UNSUPPORTED = 8       /* valid request this library does not support */
 };
 
 /* ---- context ---- */

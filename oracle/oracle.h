@@ -8,7 +8,7 @@
  * (src/vector.c).  Each function cites the reference lines it follows.
  *
  * Only the test suite, the smoke check and the CPU-baseline leg of the
- * benchmark may call into this code, and only as the checker.  The product
+ * benchmark may call into this code, and only to compare against.  The product
  * library (libvkhel.so) never links or loads it.
  *
  * Parity pin: the oracle is checked against every golden vector of the

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/oracle.c) -- TEST INFRASTRUCTURE ONLY.
 
 Used by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg,
-always as the checker or the timed CPU baseline, never as part of the product.
+always to compare against or as the timed CPU baseline, never as part of the product.
 ``load()`` builds oracle/_build/liboracle.so with make if it is missing.
 """
 import ctypes

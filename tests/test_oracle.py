@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's own golden vectors and known answers.
 
-The oracle (oracle/oracle.c) is the checker for every GPU parity test, so it
+The oracle (oracle/oracle.c) is what every GPU parity test compares with, so it
 is pinned here first: every operation recorded from the reference's
 test/vector.c, every known answer of test/numbers.c and test/ntt.c, and the
 reference's own twiddle tables (tests/golden/*.json, made by
