@@ -70,6 +70,18 @@ __device__ __forceinline__ u64 ref_reduce64(u64 x, u64 mod, u64 mu, u32 n) {
   return z >= mod ? z - mod : z;
 }
 
+// The same for operands that are usually reduced already.  For x < mod the
+// estimate floor(k mu / 2^64), k = x >> (n - 2) <= 3, mu <= 2^63, is 0: it
+// needs k mu >= 2^64, i.e. k = 2 with mod = 2^(n-1) (but x < mod gives
+// k <= 1 then) or k = 3 with mod <= 3 2^(n-2) (but x < mod gives k <= 2
+// then).  So reduce64 returns x there, the shortcut gives the same word for
+// every 64-bit x, and canonical operands skip the multiplies (the branch is
+// uniform across a warp of them).
+__device__ __forceinline__ u64 ref_reduce64_maybe(u64 x, u64 mod, u64 mu, u32 n) {
+  if (__builtin_expect(x < mod, 1)) return x;
+  return ref_reduce64(x, mod, mu, n);
+}
+
 // reduce128 (elemmul.comp:49-60).  A shift by 64 (only for a 2-bit modulus,
 // where the high word is zero) yields zero.
 __device__ __forceinline__ u64 ref_reduce128(u64 hi, u64 lo, u64 mod, u64 mu, u32 n) {
@@ -96,7 +108,7 @@ __device__ __forceinline__ u64 barrett_mul_lazy(u64 x, u64 y, u64 q, u64 q2, u64
 //   elemgtadd    src/kernels/shaders/elemgtadd.comp:20-30
 //   elemmodbytwo src/kernels/shaders/elemmodbytwo.comp:19-27 (sb = q / 2)
 __device__ __forceinline__ u64 ref_gtsub(u64 a, u64 bound, u64 d, u64 mod, u64 mu, u32 bits) {
-  const u64 r = ref_reduce64(a, mod, mu, bits);
+  const u64 r = ref_reduce64_maybe(a, mod, mu, bits);
   if (a > bound) {
     const u64 z = r + mod - d;
     return z >= mod ? z - mod : z;

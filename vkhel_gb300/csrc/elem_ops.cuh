@@ -18,8 +18,8 @@ struct OpMul {
   u64 mod, mu;
   u32 bits;
   __device__ __forceinline__ u64 operator()(u64 a, u64 b) const {
-    const u64 x = ref_reduce64(a, mod, mu, bits);
-    const u64 y = ref_reduce64(b, mod, mu, bits);
+    const u64 x = ref_reduce64_maybe(a, mod, mu, bits);
+    const u64 y = ref_reduce64_maybe(b, mod, mu, bits);
     return ref_reduce128(mulhi(x, y), x * y, mod, mu, bits);
   }
 };
@@ -47,10 +47,10 @@ struct OpFmaCanon {
   u64 m, ms, mod, mu;
   u32 bits;
   __device__ __forceinline__ u64 operator()(u64 a, u64 b) const {
-    const u64 x = ref_reduce64(a, mod, mu, bits);
+    const u64 x = ref_reduce64_maybe(a, mod, mu, bits);
     const u64 p = bits < 64 ? shoup(x, m, ms, mod)
                             : (u64)(((unsigned __int128)x * m) % mod);
-    const u64 y = ref_reduce64(b, mod, mu, bits);
+    const u64 y = ref_reduce64_maybe(b, mod, mu, bits);
     const u64 s = p + y;
     return (s < p || s >= mod) ? s - mod : s;
   }
