@@ -142,3 +142,19 @@ def test_oracle_matches_reference_numbers_c_on_random_inputs(oracle):
             assert oracle.mulmod(a, b, q) == L.nt_multiply_mod(a, b, q, 0)
             if a:
                 assert oracle.invmod(a, q) == L.nt_inverse_mod(a, q)
+
+
+def test_reference_reduce64_returns_reduced_operands_unchanged(oracle):
+    """The reference's Barrett reduce64 (elemgtsub.comp:36-47; elemgtsub with
+    a bound no word exceeds returns it) gives back every x < mod unchanged,
+    for moduli of every bit length; the element-wise kernels rely on this to
+    skip the reduction of operands that are already reduced."""
+    rng = np.random.default_rng(17)
+    for bits in range(2, 65):
+        lo, hi = 1 << (bits - 1), (1 << bits) - 1
+        mods = {max(lo, 2), hi, lo + (hi - lo) // 2, min(hi, 3 << (bits - 2)), min(hi, (3 << (bits - 2)) + 1)}
+        for mod in sorted(m for m in mods if m >= 2):
+            x = rng.integers(0, mod, size=512, dtype=np.uint64)
+            x[:4] = [0, mod - 1, mod // 2, (3 * mod) // 4]
+            out = oracle.elemgtsub(x, (1 << 64) - 1, 0, mod)
+            np.testing.assert_array_equal(out, x, err_msg=f"mod={mod}")
