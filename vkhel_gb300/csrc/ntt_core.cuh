@@ -468,11 +468,16 @@ __device__ __forceinline__ void store16(const u64 (&v)[16], u64* p) {
 }
 
 // Resident CTAs per SM the register budget is sized for: 512 threads per SM
-// (128 registers per thread) for the 32-words-per-thread shapes, 384 threads
-// (about 170 registers) for the 16-words-per-thread shapes.
-template <int LOGN, int E>
+// (128 registers per thread, 16 warps) for the 32-words-per-thread shapes and
+// for the 16-words-per-thread transforms from n = 2^9 and polymuls from
+// n = 2^12; 384 threads (about 170 registers) for the other 16-word shapes.
+// Left at 384, the 2^12 shapes took 222 registers (one CTA of 256 threads per
+// SM): 128 made them 9 % (polymul) and 17 % (transforms) faster; the 2^9 ..
+// 2^11 transforms gained 4 %, the polymuls of those sizes lost 2-3 %, and
+// n = 2^8 (16-thread CTAs) spills above 384.
+template <int LOGN, int E, bool POLY = false>
 constexpr int min_blocks() {
-  constexpr int budget = E >= 32 ? 512 : 384;
+  constexpr int budget = E >= 32 || LOGN >= (POLY ? 12 : 9) ? 512 : 384;
   return (budget / ((1 << LOGN) / E)) < 1 ? 1 : (budget / ((1 << LOGN) / E));
 }
 
@@ -560,7 +565,7 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
 // rest of the inverse transform then writes c.  a is prefetched
 // into L2 while b is transformed, the next job's b while a is.
 template <int LOGN, int E, int U, bool LIFT = false>
-__global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
+__global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E, true>())
     k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one,
               const __grid_constant__ vkcu_lift lift) {
   using S = Shape<LOGN, E, U>;
