@@ -279,9 +279,14 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 	if (err) { /* the micro-batch's requests fail; what was enqueued still drains */
 		for (uint32_t i = 0; i < sl->nreqs; i++)
 			sl->reqs[i]->status = err;
-		if (issued) { /* frees below: after every upload issued so far */
+		if (issued) { /* frees below: after every upload and kernel enqueued so far */
 			vkcu_event_record(sl->ev_done, s->s_in);
 			vkcu_stream_wait(s->s_out, sl->ev_done);
+			for (uint32_t cc = 0; cc <= c && cc < nchunks; cc++) {
+				void *cs = cc == 0 ? s->s_comp : s->s_chunk[cc - 1];
+				vkcu_event_record(sl->ev_comp[cc], cs);
+				vkcu_stream_wait(s->s_out, sl->ev_comp[cc]);
+			}
 		}
 	}
 	for (uint32_t i = 0; i < sl->nreqs; i++) {
