@@ -770,7 +770,9 @@ def main():
                 "frac": hbm_ach / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "kernel": "k_polymul<14,32>",
                 "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": kernel_ms,
-                "launch_ms_source": "mean of CUDA-event durations of isolated launches"}
+                "launch_ms_source": "mean of CUDA-event durations of isolated launches",
+                "note": "HBM is not this kernel's binding roof: it is integer-pipe bound (roofline_int; "
+                        "traffic is at the algorithmic bytes, c and NTT(b) staying in L2)"}
     int_ach = modmuls / (kernel_ms * 1e-3) / 1e9
     int_ach_eff = modmuls / (eff_ms * 1e-3) / 1e9
     roofline_int = {"bound": "int", "achieved": int_ach, "peak": bfly_peak / 1e9, "unit": "Gmodmul/s",
