@@ -541,8 +541,9 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
                   S::N * 2);
     }
     const u32 tw_mult = (1u << sub_log) + sub;
-    // first inverse pass (global stage m = n/2 first, exact rule) from global
-#pragma unroll 1
+    // first inverse pass (global stage m = n/2 first, exact rule) from global;
+    // U groups in flight, as in the other passes
+#pragma unroll(S::U)
     for (int i = 0; i < S::E / 16; i++) {
       const int g = (int)threadIdx.x + i * S::T;
       u64 v[16];
