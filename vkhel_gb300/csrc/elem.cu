@@ -23,27 +23,42 @@ namespace vk {
 // B == nullptr for unary operations.  Each thread moves P 16-byte pairs of
 // every operand per iteration (2 for binary ops, 4 for unary ones, so both
 // keep about the same bytes in flight), all loads issued before the first
-// store; lanes past the end re-read the last pair and store nothing.
+// store, and the next iteration's loads issued before this one's arithmetic
+// (2-3.4 % faster for the ops with multiplies, 0.8 % slower for elemgtadd);
+// lanes past the end re-read the last pair and store nothing.
 template <class Op, bool BIN>
 __global__ void __launch_bounds__(256) k_elementwise(u64* __restrict__ res, const u64* a, const u64* b, u64 len,
                                                      Op op) {
   constexpr int P = BIN ? 2 : 4;
   const u64 pairs = len >> 1;
   const u64 step = (u64)gridDim.x * blockDim.x * P;
-  for (u64 g0 = (u64)blockIdx.x * blockDim.x * P; g0 < pairs; g0 += step) {
-    ulonglong2 x[P], y[BIN ? P : 1];
+  const u64 first = (u64)blockIdx.x * blockDim.x * P;
+  ulonglong2 x[P], y[BIN ? P : 1];
+  // software pipelined: the next group's loads are in flight while this
+  // group is computed and stored
+  auto load = [&](u64 g0, ulonglong2(&xs)[P], ulonglong2(&ys)[BIN ? P : 1]) {
 #pragma unroll
     for (int k = 0; k < P; k++) {
       const u64 p = g0 + threadIdx.x + (u64)k * blockDim.x;
       const u64 pc = p < pairs ? p : pairs - 1;
-      x[k] = ld2(a + 2 * pc);
-      if constexpr (BIN) y[k] = ld2(b + 2 * pc);
+      xs[k] = ld2(a + 2 * pc);
+      if constexpr (BIN) ys[k] = ld2(b + 2 * pc);
     }
+  };
+  if (first < pairs) load(first, x, y);
+  for (u64 g0 = first; g0 < pairs; g0 += step) {
+    ulonglong2 xn[P], yn[BIN ? P : 1];
+    if (g0 + step < pairs) load(g0 + step, xn, yn);
 #pragma unroll
     for (int k = 0; k < P; k++) {
       const u64 p = g0 + threadIdx.x + (u64)k * blockDim.x;
       const ulonglong2 yk = BIN ? y[BIN ? k : 0] : make_ulonglong2(0, 0);
       if (p < pairs) st2(res + 2 * p, op(x[k].x, yk.x), op(x[k].y, yk.y));
+    }
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+      x[k] = xn[k];
+      if constexpr (BIN) y[k] = yn[BIN ? k : 0];
     }
   }
   if ((len & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
