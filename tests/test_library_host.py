@@ -145,3 +145,38 @@ def test_tables_dbgprint_matches_reference_format(vk, oracle, capfd):
               f"\troots_of_unity: {', '.join(str(int(x)) for x in ref['roots'])}\n"
               f"\tinv_roots_of_unity: {', '.join(str(int(x)) for x in ref['inv_roots'])}\n")
     assert out == expect
+
+
+def test_tuning_table_parsing_and_overrides(vk, tmp_path):
+    """The variant table: "family log_n variant" lines, '#' comments, lines
+    that do not parse or name an unknown family / degree / a negative variant
+    ignored; vkhel_tune_set / _get at run time; the committed GB300 table
+    names a variant for every CTA-resident degree of the three kernel
+    families and the concurrent-classes flag.  (Host only: no device.)"""
+    L = vk.lib()
+    table = os.path.join(ROOT, "vkhel_gb300", "tuning", "gb300.txt")
+    saved = {(f, n): L.vkhel_tune_get(f, n) for f in range(4) for n in range(32)}
+    try:
+        t = tmp_path / "table.txt"
+        t.write_text("# comment line\n0 14 1   # trailing comment\n1 13 2\nnot a line\n"
+                     "9 10 1\n0 40 1\n2 12 -1\n2 11 1 extra\n")
+        assert L.vkhel_tune_load(str(t).encode()) == 0
+        assert L.vkhel_tune_get(0, 14) == 1 and L.vkhel_tune_get(1, 13) == 2 and L.vkhel_tune_get(2, 11) == 1
+        assert L.vkhel_tune_get(2, 12) == saved[(2, 12)]       # negative variant ignored
+        assert L.vkhel_tune_load(str(tmp_path / "missing.txt").encode()) != 0
+        assert L.vkhel_tune_set(3, 1, 1) == 0 and L.vkhel_tune_get(3, 1) == 1
+        assert L.vkhel_tune_set(4, 1, 1) != 0 and L.vkhel_tune_set(0, 32, 1) != 0 and L.vkhel_tune_set(0, 1, -1) != 0
+        lib_clear_error = getattr(L, "vkhel_ctx_clear_error", None)
+        if lib_clear_error:
+            lib_clear_error(None)
+        entries = set()
+        for line in open(table):
+            line = line.split("#")[0].split()
+            if len(line) == 3:
+                entries.add((int(line[0]), int(line[1])))
+        for fam in (0, 1, 2):
+            assert {(fam, n) for n in range(8, 15)} <= entries, f"family {fam} incomplete"
+        assert (3, 0) in entries
+    finally:
+        for (f, n), v in saved.items():
+            L.vkhel_tune_set(f, n, v)
