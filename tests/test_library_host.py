@@ -180,3 +180,32 @@ def test_tuning_table_parsing_and_overrides(vk, tmp_path):
     finally:
         for (f, n), v in saved.items():
             L.vkhel_tune_set(f, n, v)
+
+
+def test_lazy_host_tables_under_concurrent_first_requests(vk, oracle):
+    """Tables the device can generate (q < 2^61) build their host arrays only
+    on first request, under a lock: eight threads asking for them at once
+    (ctypes releases the GIL during the call) all get the oracle's arrays.
+    Host only: no device."""
+    import threading
+    n = 1 << 14
+    q = workloads.ntt_primes(n, 1)[0]
+    w = workloads.root_for(n, q)
+    ref = oracle.tables(n, q, w)
+    for _ in range(3):  # fresh tables each round: the first request races
+        t = vk.NttTables(n, q, w)
+        results, go = [None] * 8, threading.Barrier(8)
+
+        def worker(i):
+            go.wait()
+            results[i] = t.arrays()
+
+        threads = [threading.Thread(target=worker, args=(i,)) for i in range(8)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        for r in results:
+            for k, v in ref.items():
+                np.testing.assert_array_equal(r[k], v, err_msg=k)
+        t.close()
