@@ -255,3 +255,22 @@ def test_polymul_is_negacyclic_schoolbook(vk, ctx, oracle, log_n):
     a, b, c = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h), vk.Vector(ctx, n)
     vk.polymul(a, b, c, vk.NttTables(n, q, w))
     np.testing.assert_array_equal(c.download(), oracle.schoolbook(a_h, b_h, n, q))
+
+
+def test_zero_length_results(vk, ctx):
+    """Zero-length vectors, which the reference allows: every element-wise op
+    with a zero-length result does nothing and reports no error, also with
+    longer operands; the vectors download as empty arrays."""
+    q = (1 << 61) - 1
+    a, b, r = vk.Vector(ctx, 0), vk.Vector(ctx, 0), vk.Vector(ctx, 0)
+    x = vk.Vector(ctx, np.arange(1, 9, dtype=np.uint64))
+    for p, s in ((a, b), (x, x)):
+        vk.elemmul(p, s, r, q)
+        vk.elemfma(p, s, r, 3, q)
+        vk.elemfma_canonical(p, s, r, 3, q)
+        vk.elemgtadd(p, r, 1, 2)
+        vk.elemgtsub(p, r, 1, 2, q)
+        vk.elemmod(p, r, 65537, q)
+        vk.elemmod(p, r, 2, q)
+    assert r.download().size == 0 and a.download().size == 0
+    np.testing.assert_array_equal(x.download(), np.arange(1, 9, dtype=np.uint64))
