@@ -137,16 +137,19 @@ int vkhel_vector_inverse_transform_lift(const struct vkhel_vector *a,
 		const struct vkhel_lift_step *steps, uint32_t nsteps);
 
 /* Same product as vkhel_vector_polymul without allocating any device memory
- * (no counterpart in the reference).  For callers that may not allocate at
- * the call site -- e.g. while a stream is being captured into a CUDA graph, or
- * inside another component's fixed memory budget -- the kernel's NTT(b)
- * scratch is a static device array of 16384 words (128 KiB per device, kept
- * until exit) instead of a pool buffer.  Needs 256 <= n <= 16384 and the
- * tables already resident on the context (any earlier transform, polymul or
- * batch call with them); rejects other sizes with VKHEL_ERR_UNSUPPORTED.
+ * (no counterpart in the reference).  For callers that cannot let the library
+ * allocate where they multiply -- a program whose device memory is all held
+ * by its own allocator or a fixed per-tenant reservation, or a latency-
+ * critical loop that must not call cudaMalloc / cudaFree, which can wait for
+ * queued device work -- the kernel's NTT(b) scratch is a static device array
+ * of 16384 words (128 KiB per device, kept until exit) instead of a pool
+ * buffer.  Needs 256 <= n <= 16384 (other sizes: VKHEL_ERR_UNSUPPORTED) and
+ * the tables already resident on the context through an earlier transform,
+ * polymul or batch call with them (otherwise VKHEL_ERR_INVALID_ARGUMENT).
  * All calls share the array: calls that overlap on the GPU race.  The first
- * call on a device looks up the array's address; make it before any stream
- * capture.  Synchronous; returns a status. */
+ * call on a device looks up the array's address and first launches the
+ * kernel for its degree; make it during set-up, before any stream capture.
+ * Synchronous; returns a status. */
 int vkhel_vector_polymul_noalloc(const struct vkhel_vector *a,
 		const struct vkhel_vector *b, struct vkhel_vector *result,
 		const struct vkhel_ntt_tables *ntt);

@@ -137,6 +137,18 @@ class Oracle:
         return c, used
 
 
+def reference_dir():
+    """The reference checkout's location as oracle/Makefile resolves it
+    (VKHEL_REF overrides it), or None where it is absent (GPU machines)."""
+    try:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"],
+                           capture_output=True, text=True, timeout=30)
+    except (OSError, subprocess.SubprocessError):
+        return None
+    d = r.stdout.strip()
+    return d if r.returncode == 0 and d and os.path.isdir(os.path.join(d, "src")) else None
+
+
 _oracle = None
 
 

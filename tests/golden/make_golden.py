@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run from the repository root, in a container that has the reference at
-/root/reference (override with VKHEL_REF=...):
+Run from the repository root, in a container that has the reference checkout
+(oracle/Makefile knows its usual location; override with VKHEL_REF=...):
 
     python tests/golden/make_golden.py
 
@@ -34,7 +34,12 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("VKHEL_REF", "/root/reference")
+sys.path.insert(0, ROOT)
+from oracle import pyoracle  # noqa: E402
+
+REF = pyoracle.reference_dir()
+if REF is None:
+    raise SystemExit("the reference checkout is not present (set VKHEL_REF=...)")
 
 
 def build_ref():

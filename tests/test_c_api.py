@@ -107,10 +107,15 @@ def test_c_extension_program_checks_pass(vk, tmp_path):
 # only its public header.  Where the reference's sources are present (they
 # are not on GPU machines) they must compile against include/vkhel/vkhel.h
 # and link against libvkhel.so unchanged: the source-level drop-in check.
-REFERENCE_SRC = os.environ.get("VKHEL_REFERENCE_SRC", "/root/reference")
+def _reference_src():
+    from oracle import pyoracle
+    return pyoracle.reference_dir()
 
 
-@pytest.mark.skipif(not os.path.isfile(os.path.join(REFERENCE_SRC, "test", "vector.c")),
+REFERENCE_SRC = _reference_src()
+
+
+@pytest.mark.skipif(REFERENCE_SRC is None or not os.path.isfile(os.path.join(REFERENCE_SRC, "test", "vector.c")),
                     reason="the reference's sources are not present on this machine")
 @pytest.mark.parametrize("src", ["test/vector.c", "examples/example.c"])
 def test_reference_programs_compile_and_link_unchanged(vk, tmp_path, src):

@@ -1,16 +1,18 @@
-"""vkhel_vector_polymul_noalloc: the polynomial multiply for callers that may
-not allocate device memory where they call it (for example while a stream is
-being captured into a CUDA graph, or inside a fixed memory budget owned by
-another component).
+"""vkhel_vector_polymul_noalloc: the polynomial multiply for callers that
+cannot let the library allocate device memory where they multiply (their
+device memory is all held by their own allocator or a fixed reservation, or
+a latency-critical loop must not call cudaMalloc / cudaFree, which can wait
+for queued device work).
 
 The entry point keeps its NTT(b) scratch in a static device array instead of
 asking the context's pool for it.  This test calls it through the C ABI twice
 in a row, on a fresh context whose budget is frozen at the bytes already in
 use (so any pool allocation would fail), and checks each result bit for bit
-against the allocating entry point vkhel_vector_polymul.  The tolerance is
-zero: the products are integer arithmetic.  The file is named to be collected
-last and uses only its own context, so it passes alone or after the rest of
-the suite.
+against the allocating entry point vkhel_vector_polymul and against the CPU
+oracle's polymul, for a 60-bit prime and for the largest NTT prime below
+2^62 (the top of the kernel's modulus range).  The tolerance is zero: the
+products are integer arithmetic.  The file is named to be collected last and
+uses only its own context, so it passes alone or after the rest of the suite.
 """
 import numpy as np
 import pytest
@@ -20,10 +22,11 @@ from vkhel_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("qbound", [1 << 60, 1 << 62])
 @pytest.mark.parametrize("log_n", [8, 12, 14])
-def test_noalloc_polymul_equals_allocating_polymul(vk, log_n):
+def test_noalloc_polymul_equals_allocating_polymul(vk, oracle, log_n, qbound):
     n = 1 << log_n
-    q = workloads.ntt_primes(n, 1)[0]
+    q = workloads.ntt_primes(n, 1, bound=qbound)[0]
     w = workloads.root_for(n, q)
     rng = np.random.default_rng(1000 + log_n)
     with vk.Context() as ctx:
@@ -41,7 +44,11 @@ def test_noalloc_polymul_equals_allocating_polymul(vk, log_n):
                 b.upload(b_h)
                 vk.polymul(a, b, ref, t)
             vk.polymul_noalloc(a, b, got, t)
-            np.testing.assert_array_equal(got.download(), ref.download(), err_msg=f"call {call}")
+            g = got.download()
+            np.testing.assert_array_equal(g, ref.download(), err_msg=f"call {call}")
+            want, st = oracle.polymul(a_h, b_h, n, q, w)
+            assert st == 0
+            np.testing.assert_array_equal(g, want, err_msg=f"call {call} vs the oracle")
         # result aliasing an operand is fine: the scratch is separate
         vk.polymul_noalloc(a, b, a, t)
         np.testing.assert_array_equal(a.download(), ref.download())

@@ -1,29 +1,34 @@
 // Fused polynomial multiply for callers that cannot allocate device memory.
 //
 // vkhel_vector_polymul parks NTT(b) in the result vector, or in a temporary
-// buffer from the context's pool when the result aliases a.  Some callers may
-// not allocate at all at the point where they multiply: code that runs while
-// a stream is being captured into a CUDA graph (allocation calls are not
-// allowed there), code inside another library's memory budget that owns all
-// of the device memory it may touch, or latency-critical serving paths that
-// must not call into the allocator.  vkhel_vector_polymul_noalloc runs the
-// same kernel (k_polymul) with its scratch in this file's static device array
-// instead, so it allocates nothing: the caller passes inputs and outputs.
+// buffer from the context's pool when the result aliases a.  Some callers
+// cannot let the library allocate at the point where they multiply: a host
+// program that has already handed all the device memory it may use to its
+// own allocator (another framework's caching allocator, a fixed reservation
+// per tenant), so that a pool allocation would fail or push it over its
+// limit; or a latency-critical loop that must not call cudaMalloc / cudaFree,
+// which can stall until work already queued on the device has drained.
+// vkhel_vector_polymul_noalloc runs the same kernel (k_polymul) with its
+// scratch in this file's static device array instead, so it allocates
+// nothing: the caller passes inputs and outputs.
 //
 // Limits and rules:
 //   * degree 256 <= n <= kNoallocMaxWords (16384): the fused range; the
 //     scratch array is kNoallocMaxWords words (128 KiB) on every device that
-//     loads libvkhel, held until the process exits;
+//     loads libvkhel, held until the process exits; larger n is rejected with
+//     VKHEL_ERR_UNSUPPORTED;
 //   * the twiddle tables must already be resident on the context (any
 //     transform, polymul or batch call with them uploads them); otherwise the
-//     call fails instead of uploading (which would allocate);
+//     call fails with VKHEL_ERR_INVALID_ARGUMENT instead of uploading (which
+//     would allocate);
 //   * every call on a device shares the one array and the kernel overwrites
 //     the n words it uses before reading them (nothing needs clearing), so
 //     calls that overlap on the GPU -- two contexts or threads running it at
 //     once -- race on the array; calls must not overlap;
 //   * the first call on each device resolves the array's device address with
 //     cudaGetSymbolAddress (host code cannot use the array's name as a device
-//     pointer); make that first call before any stream capture.
+//     pointer) and is the first launch of the kernel for its degree; make
+//     that first call during set-up, before any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
