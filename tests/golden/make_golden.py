@@ -36,6 +36,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from oracle import pyoracle  # noqa: E402
+from vkhel_gb300 import workloads  # noqa: E402
 
 REF = pyoracle.reference_dir()
 if REF is None:
@@ -135,11 +136,19 @@ def reference_tables():
         (4096, 1152921504606830593, 431606828070683274),
         (16384, 1152921504606748673, 641000223749548346),
         (65536, 1152921504606584833, None),
+        # the top of the modulus range (2^62 <= q < 2^63): the first such
+        # primes below 2^63 (at n = 256 the reference's Barrett products
+        # overflow there, so its "powers" of w are not w^i) and above 2^62,
+        # and a degree past 2^18
+        (256, _ntt_prime(256, 1 << 63, down=True), None),
+        (4096, _ntt_prime(4096, 1 << 63, down=True), None),
+        (16384, _ntt_prime(16384, 1 << 62, down=False), None),
+        (1 << 20, _ntt_prime(1 << 20, 1 << 60, down=True), None),
     ]
     out = []
     for n, q, w in sets:
-        if w is None:
-            w = _root_for(lib, n, q)
+        if w is None:  # exact arithmetic (the reference's own powers overflow at 63 bits)
+            w = workloads.root_for(n, q)
         t = lib.vkhel_ntt_tables_create(n, q, w).contents
         arrays = {k: [getattr(t, k)[i] for i in range(n)]
                   for k in ("roots", "inv_roots", "roots_shoup", "inv_roots_shoup")}
@@ -153,14 +162,14 @@ def reference_tables():
     return out
 
 
-def _root_for(lib, n, q):
-    lib.nt_power_mod.restype = ctypes.c_uint64
-    lib.nt_power_mod.argtypes = [ctypes.c_uint64] * 3
-    for x in range(2, 1000):
-        w = lib.nt_power_mod(x, (q - 1) // (2 * n), q)
-        if lib.nt_power_mod(w, n, q) == q - 1:
-            return w
-    raise ValueError("no root")
+def _ntt_prime(n, bound, down):
+    """The first prime q = 1 (mod 2n) below (down) or above `bound`."""
+    if down:
+        return workloads.ntt_primes(n, 1, bound=bound)[0]
+    q = (bound // (2 * n)) * (2 * n) + 1
+    while not workloads.is_prime(q):
+        q += 2 * n
+    return q
 
 
 def main():

@@ -107,9 +107,13 @@ def ntt_params(n, bits):
     return q, workloads.root_for(n, q)
 
 
-@pytest.mark.parametrize("log_n", list(range(1, 18)))
-@pytest.mark.parametrize("bits", [31, 60, 62])
+@pytest.mark.parametrize("log_n", list(range(1, 21)))
+@pytest.mark.parametrize("bits", [31, 60, 62, 63])
 def test_transforms_match_oracle(vk, ctx, oracle, log_n, bits):
+    """Every degree 2..2^20 (one CTA, a cluster, passes over HBM) for 31- to
+    63-bit primes; the 63-bit ones (2^62 <= q < 2^63) run the [0, 2q) kernel
+    family, and below 2^63 by a little the reference's own table products
+    overflow, so its tables are not the powers of w (they are reproduced)."""
     n = 1 << log_n
     if bits == 31 and n >= 1 << 14:
         bits = 40
@@ -133,11 +137,12 @@ def test_transforms_match_oracle(vk, ctx, oracle, log_n, bits):
     np.testing.assert_array_equal(v.download(), f_ref)
 
 
-@pytest.mark.parametrize("log_n", [1, 3, 7, 8, 10, 13, 14, 15, 16])
-def test_forward_unreduced_inputs_match_oracle(vk, ctx, oracle, log_n):
+@pytest.mark.parametrize("bits", [61, 63])
+@pytest.mark.parametrize("log_n", [1, 3, 7, 8, 10, 13, 14, 15, 16, 18, 19])
+def test_forward_unreduced_inputs_match_oracle(vk, ctx, oracle, log_n, bits):
     # the first reference stage wraps (X + WY) at 2^64 before reducing
     n = 1 << log_n
-    q, w = ntt_params(n, 61)
+    q, w = ntt_params(n, bits)
     rng = np.random.default_rng(log_n)
     a_h = rand64(rng, n)
     a_h[: min(n, 8)] = edge_values(q)[: min(n, 8)]
@@ -149,12 +154,13 @@ def test_forward_unreduced_inputs_match_oracle(vk, ctx, oracle, log_n):
     np.testing.assert_array_equal(r.download(), f_ref)
 
 
-@pytest.mark.parametrize("log_n", [1, 4, 8, 11, 14, 15])
-def test_inverse_unreduced_inputs_match_oracle(vk, ctx, oracle, log_n):
+@pytest.mark.parametrize("bits", [60, 63])
+@pytest.mark.parametrize("log_n", [1, 4, 8, 11, 14, 15, 18, 19])
+def test_inverse_unreduced_inputs_match_oracle(vk, ctx, oracle, log_n, bits):
     # inputs below 2^62 (the reference's subtraction loop terminates) plus
     # pairs whose sum wraps 2^64 with a small second element
     n = 1 << log_n
-    q, w = ntt_params(n, 60)
+    q, w = ntt_params(n, bits)
     rng = np.random.default_rng(log_n + 7)
     a_h = rng.integers(0, 1 << 62, size=n, dtype=np.uint64)
     if n >= 4:
@@ -202,20 +208,29 @@ def test_transform_degree_one(vk, ctx, oracle):
 
 def test_transform_rejects_unsupported(vk, ctx):
     n = 16
-    t = vk.NttTables(n, (1 << 62) + 1, 3)
-    a = vk.Vector(ctx, n)
+    t = vk.NttTables(n, (1 << 63) + 1, 3)  # the reference's inverse-mod needs q < 2^63
+    a = vk.Vector(ctx, 64)
     with pytest.raises(vk.VkhelError) as e:
         vk.forward_transform(a, a, t)
     assert e.value.code == 8
+    # a 63-bit modulus whose reference table builder leaves an entry >= q
+    # (its Barrett product overflows): refused rather than computed lazily
+    t = vk.NttTables(64, 8735340036816624049, 8488042347404613068)
+    assert (t.arrays()["roots"] >= t.q).any()
+    with pytest.raises(vk.VkhelError) as e:
+        vk.forward_transform(a, a, t)
+    assert e.value.code == 8 and "not below q" in e.value.msg
     t = vk.NttTables(32, 2251799813685313, 3)
     with pytest.raises(vk.VkhelError):
         vk.forward_transform(a, a, t)  # vector shorter than n
 
 
-@pytest.mark.parametrize("log_n", [17])
+@pytest.mark.parametrize("log_n", [17, 22, 24])
 def test_round_trip_largest_degree(vk, ctx, log_n):
     n = 1 << log_n
-    for bits in (40, 60, 62):
+    # 62- and 63-bit tables are built on the host (63-bit: one extended-Euclid
+    # inverse per entry, as the reference does), seconds at 2^24
+    for bits in (40, 60, 62, 63) if log_n < 24 else (40, 60):
         q, w = ntt_params(n, bits)
         t = vk.NttTables(n, q, w)
         a_h = workloads.uniform(np.random.default_rng(bits), q, n)
@@ -226,10 +241,15 @@ def test_round_trip_largest_degree(vk, ctx, log_n):
         np.testing.assert_array_equal(v.download(), a_h)
 
 
-@pytest.mark.parametrize("log_n", [1, 2, 4, 7, 8, 9, 10, 12, 13, 14, 15, 16])
-def test_polymul_matches_reference_composition(vk, ctx, oracle, log_n):
+@pytest.mark.parametrize("bits", [60, 63])
+@pytest.mark.parametrize("log_n", [1, 2, 4, 7, 8, 9, 10, 12, 13, 14, 15, 16, 17, 18, 20])
+def test_polymul_matches_reference_composition(vk, ctx, oracle, log_n, bits):
+    """The fused (2^8..2^17) and composed (other n) products equal the
+    reference's forward, forward, elemmul, inverse; at 63 bits elemmul's
+    Barrett estimate overflows for large products and the kernels reproduce
+    its words."""
     n = 1 << log_n
-    q, w = ntt_params(n, 60)
+    q, w = ntt_params(n, bits)
     t = vk.NttTables(n, q, w)
     rng = np.random.default_rng(log_n + 40)
     a_h, b_h = workloads.uniform(rng, q, n), workloads.uniform(rng, q, n)

@@ -65,7 +65,8 @@ def test_host_tables_equal_reference_tables(vk, rec):
         assert hashlib.sha256(v.astype("<u8").tobytes()).hexdigest() == rec[k + "_sha256"], k
 
 
-@pytest.mark.parametrize("n,bits", [(2, 20), (8, 30), (256, 40), (4096, 61), (1024, 62)])
+@pytest.mark.parametrize("n,bits", [(2, 20), (8, 30), (256, 40), (4096, 61), (1024, 62), (256, 63), (4096, 63),
+                                    (16384, 63)])
 def test_host_tables_equal_oracle(vk, oracle, n, bits):
     q = workloads.ntt_primes(n, 1, bound=1 << bits)[0]
     w = workloads.root_for(n, q)

@@ -319,6 +319,19 @@ class Vector:
         data = _as_u64(data)
         _status(self.ctx.ptr, lib().vkhel_vector_upload(self.ptr, data.ctypes.data, data.size))
 
+    def upload_async(self, host, count=None):
+        """vkhel_vector_upload_async: enqueue a copy of `count` words (all of
+        `host` by default) from a uint64 numpy array or a torch tensor; `host`
+        must stay alive and unchanged until the context is synchronized."""
+        count = (host.size if isinstance(host, np.ndarray) else host.numel()) if count is None else count
+        _status(self.ctx.ptr, lib().vkhel_vector_upload_async(self.ptr, _ptr(host), int(count)))
+
+    def download_async(self, host, count=None):
+        """vkhel_vector_download_async into `host` (uint64 numpy array or torch
+        tensor); the words are there once the context is synchronized."""
+        count = (host.size if isinstance(host, np.ndarray) else host.numel()) if count is None else count
+        _status(self.ctx.ptr, lib().vkhel_vector_download_async(self.ptr, _ptr(host), int(count)))
+
     def copy_from_host(self, data):
         data = _as_u64(data)
         assert data.size >= self.length

@@ -474,8 +474,12 @@ static int check_transform(const char *op, const struct vkhel_vector *a, const s
 	if (a->length < t->n || res->length < t->n)
 		return vkh_fail(res->ctx, VKHEL_ERR_INVALID_ARGUMENT,
 				"%s: vectors of %" PRIu64 "/%" PRIu64 " words for n=%" PRIu64, op, a->length, res->length, t->n);
-	if (t->q >= ((uint64_t) 1 << 62) || t->q < 3)
-		return vkh_fail(res->ctx, VKHEL_ERR_UNSUPPORTED, "%s: q=%" PRIu64 " outside [3, 2^62)", op, t->q);
+	/* the reference's inverse-mod and butterfly sums hold below 2^63
+	 * (src/numbers.c:71-99, nttfwdbutterfly.comp:44-57) */
+	if (t->q >= ((uint64_t) 1 << 63) || t->q < 3)
+		return vkh_fail(res->ctx, VKHEL_ERR_UNSUPPORTED, "%s: q=%" PRIu64 " outside [3, 2^63)", op, t->q);
+	if (t->unreduced)
+		return vkh_fail(res->ctx, VKHEL_ERR_UNSUPPORTED, "%s: a table entry is not below q=%" PRIu64, op, t->q);
 	if (t->log_n > vkcu_max_log_n())
 		return vkh_fail(res->ctx, VKHEL_ERR_UNSUPPORTED, "%s: n=%" PRIu64 " above 2^%u", op, t->n,
 				vkcu_max_log_n());
@@ -491,7 +495,7 @@ static void forward_impl(const struct vkhel_vector *a, struct vkhel_vector *res,
 	if (t->n == 1)
 		return; /* the stage loop of src/vector.c:537 runs zero times */
 	const vkcu_ntt_job job = {a->dev, res->dev, d->dev_set};
-	finish(res->ctx, vkcu_ntt_forward(res->ctx->stream, NULL, 1, &job, t->log_n, res->ctx->sms),
+	finish(res->ctx, vkcu_ntt_forward(res->ctx->stream, NULL, 1, &job, t->log_n, vkcu_wide(t->q), res->ctx->sms),
 			"forward_transform");
 }
 
@@ -516,7 +520,7 @@ static int inverse_impl(const struct vkhel_vector *a, struct vkhel_vector *res, 
 	int e = 0;
 	if (t->n > 1) {
 		const vkcu_ntt_job job = {a->dev, res->dev, d->dev_set};
-		e = vkcu_ntt_inverse_lift(ctx->stream, NULL, 1, &job, t->log_n, ctx->sms, lp);
+		e = vkcu_ntt_inverse_lift(ctx->stream, NULL, 1, &job, t->log_n, vkcu_wide(t->q), ctx->sms, lp);
 	}
 	/* src/vector.c:635-638 scales result->length words by n^-1: words past n
 	 * (and, for n == 1, the untouched result) are scaled here. */
@@ -656,18 +660,18 @@ static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector 
 	int e;
 	if (fused) {
 		const vkcu_poly_job job = {a->dev, b->dev, res->dev, scratch, d->dev_set};
-		e = vkcu_polymul_lift(ctx->stream, NULL, 1, &job, t->log_n, ctx->sms, lp);
+		e = vkcu_polymul_lift(ctx->stream, NULL, 1, &job, t->log_n, vkcu_wide(t->q), ctx->sms, lp);
 	} else {
 		const vkcu_ntt_job jb = {b->dev, scratch, d->dev_set};
 		const vkcu_ntt_job ja = {a->dev, res->dev, d->dev_set};
 		const vkcu_ntt_job jc = {res->dev, res->dev, d->dev_set};
-		e = vkcu_ntt_forward(ctx->stream, NULL, 1, &jb, t->log_n, ctx->sms);
+		e = vkcu_ntt_forward(ctx->stream, NULL, 1, &jb, t->log_n, vkcu_wide(t->q), ctx->sms);
 		if (!e)
-			e = vkcu_ntt_forward(ctx->stream, NULL, 1, &ja, t->log_n, ctx->sms);
+			e = vkcu_ntt_forward(ctx->stream, NULL, 1, &ja, t->log_n, vkcu_wide(t->q), ctx->sms);
 		if (!e)
 			e = vkcu_elemmul(ctx->stream, res->dev, res->dev, scratch, t->n, t->q, t->mu, t->qbits);
 		if (!e)
-			e = vkcu_ntt_inverse_lift(ctx->stream, NULL, 1, &jc, t->log_n, ctx->sms, lp);
+			e = vkcu_ntt_inverse_lift(ctx->stream, NULL, 1, &jc, t->log_n, vkcu_wide(t->q), ctx->sms, lp);
 	}
 	st = finish(ctx, e, "polymul");
 	if (tmp)

@@ -18,13 +18,14 @@
 
 #include "internal.h"
 
-#define MAX_CLASSES 32
+#define MAX_CLASSES 64
 
 struct job_rec {
 	uint32_t kind;         /* VKH_JOB_* */
 	uint32_t log_n;
 	uint32_t needs_scratch;
 	uint32_t lift;         /* index into the batch's lift table, 0 = none */
+	uint32_t wide;         /* modulus class: 2^62 <= q < 2^63 */
 	uint32_t order;        /* insertion order, keeps the sort stable */
 	vkcu_poly_job job;
 };
@@ -107,7 +108,7 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		const struct vkhel_ntt_tables *t = tables[k];
 		if (!t || t->n != n || n < 2)
 			return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: limb %u tables invalid", k);
-		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_log_n())
+		if (t->q >= ((uint64_t) 1 << 63) || t->q < 3 || t->unreduced || t->log_n > vkcu_max_log_n())
 			return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_add: limb %u (n, q) unsupported", k);
 	}
 	uint32_t lift_id = 0;
@@ -140,6 +141,7 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		r->log_n = log_n;
 		r->needs_scratch = kind == VKH_JOB_POLYMUL && (!fused || overlap);
 		r->lift = lift_id;
+		r->wide = (uint32_t) vkcu_wide(tables[k]->q);
 		r->order = b->njobs - 1;
 		r->job.a = ak;
 		r->job.b = kind == VKH_JOB_POLYMUL ? bk : NULL;
@@ -221,6 +223,8 @@ static int cmp_rec(const void *x, const void *y) {
 		return (a->kind > b->kind) - (a->kind < b->kind);
 	if (a->log_n != b->log_n)
 		return (a->log_n > b->log_n) - (a->log_n < b->log_n);
+	if (a->wide != b->wide)
+		return (a->wide > b->wide) - (a->wide < b->wide);
 	if (a->lift != b->lift)
 		return (a->lift > b->lift) - (a->lift < b->lift);
 	return (a->order > b->order) - (a->order < b->order);
@@ -239,21 +243,22 @@ int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, cons
 		const vkcu_ntt_job *tj = dev_ntt + 3 * (size_t) cl->first;
 		int e;
 		if (cl->kind == VKH_JOB_FORWARD) {
-			e = vkcu_ntt_forward(stream, tj, (int) cl->count, NULL, cl->log_n, sms);
+			e = vkcu_ntt_forward(stream, tj, (int) cl->count, NULL, cl->log_n, cl->wide, sms);
 		} else if (cl->kind == VKH_JOB_INVERSE) {
-			e = vkcu_ntt_inverse_lift(stream, tj, (int) cl->count, NULL, cl->log_n, sms, lift);
+			e = vkcu_ntt_inverse_lift(stream, tj, (int) cl->count, NULL, cl->log_n, cl->wide, sms, lift);
 		} else if (cl->fused) {
-			e = vkcu_polymul_lift(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, sms, lift);
+			e = vkcu_polymul_lift(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, cl->wide, sms,
+					lift);
 		} else {
 			const vkcu_ntt_job *nj = dev_ntt + 3 * (size_t) cl->first;
-			e = vkcu_ntt_forward(stream, nj, (int) cl->count, NULL, cl->log_n, sms);
+			e = vkcu_ntt_forward(stream, nj, (int) cl->count, NULL, cl->log_n, cl->wide, sms);
 			if (!e)
-				e = vkcu_ntt_forward(stream, nj + cl->count, (int) cl->count, NULL, cl->log_n, sms);
+				e = vkcu_ntt_forward(stream, nj + cl->count, (int) cl->count, NULL, cl->log_n, cl->wide, sms);
 			if (!e)
-				e = vkcu_pointwise(stream, dev_poly + cl->first, (int) cl->count, cl->log_n, sms);
+				e = vkcu_pointwise(stream, dev_poly + cl->first, (int) cl->count, cl->log_n, cl->wide, sms);
 			if (!e)
-				e = vkcu_ntt_inverse_lift(stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n, sms,
-						lift);
+				e = vkcu_ntt_inverse_lift(stream, nj + 2 * (size_t) cl->count, (int) cl->count, NULL, cl->log_n,
+						cl->wide, sms, lift);
 		}
 		if (e)
 			return e;
@@ -332,12 +337,14 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	for (uint32_t i = 0; i < b->njobs; i++) {
 		struct job_rec *r = &b->recs[i];
 		if (b->nclasses == 0 || b->classes[b->nclasses - 1].kind != r->kind ||
-				b->classes[b->nclasses - 1].log_n != r->log_n || b->classes[b->nclasses - 1].lift != r->lift) {
+				b->classes[b->nclasses - 1].log_n != r->log_n || b->classes[b->nclasses - 1].wide != (int) r->wide ||
+				b->classes[b->nclasses - 1].lift != r->lift) {
 			if (b->nclasses == MAX_CLASSES)
 				return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_commit: too many degree classes");
 			struct vkh_job_class *cl = &b->classes[b->nclasses++];
 			cl->kind = r->kind;
 			cl->log_n = r->log_n;
+			cl->wide = (int) r->wide;
 			cl->lift = r->lift;
 			cl->first = i;
 			cl->count = 0;

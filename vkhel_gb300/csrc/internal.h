@@ -62,6 +62,10 @@ struct vkhel_ntt_tables {
 	int host_ready;
 	/* q < 2^61, n >= 2 and w^n = -1: generated on the device */
 	int device_gen;
+	/* some root or inverse root is not below q (only 63-bit moduli, whose
+	 * Barrett products in the reference's table builder can overflow): the
+	 * transforms refuse these tables */
+	int unreduced;
 	uint64_t w_red; /* w mod q */
 	/* derived constants for the device twiddle set */
 	uint64_t mu, ninv, ninv_s, w1ninv, w1ninv_s;
@@ -101,6 +105,7 @@ struct vkh_job_class {
 	uint32_t log_n;
 	uint32_t first, count;
 	int fused;
+	int wide;              /* modulus class of every job: 2^62 <= q < 2^63 */
 	uint32_t lift;         /* index into the lift table, 0 = none */
 };
 /* lifts: table indexed by vkh_job_class.lift (NULL when no class has one) */

@@ -148,37 +148,42 @@ typedef struct vkcu_lift {
 } vkcu_lift;
 
 /* ---- transforms (ntt.cu) ----
- * `jobs` is a device array of `njobs` jobs that all share log_n, or NULL to
- * launch the single job `one` passed by value.  `scratch` (large n only)
- * holds njobs * n words when the transform is done in several passes. */
+ * `jobs` is a device array of `njobs` jobs that all share log_n and the
+ * modulus class, or NULL to launch the single job `one` passed by value.
+ * `wide` selects the class: 0 for q < 2^62 (lazy [0, 4q) butterflies), 1 for
+ * 2^62 <= q < 2^63 ([0, 2q) butterflies). */
+#define VKCU_WIDE_Q ((uint64_t) 1 << 62)
+static inline int vkcu_wide(uint64_t q) { return q >= VKCU_WIDE_Q; }
 int vkcu_ntt_forward(void *stream, const vkcu_ntt_job *jobs, int njobs,
-		const vkcu_ntt_job *one, uint32_t log_n, int sms);
+		const vkcu_ntt_job *one, uint32_t log_n, int wide, int sms);
 int vkcu_ntt_inverse(void *stream, const vkcu_ntt_job *jobs, int njobs,
-		const vkcu_ntt_job *one, uint32_t log_n, int sms);
+		const vkcu_ntt_job *one, uint32_t log_n, int wide, int sms);
 int vkcu_polymul(void *stream, const vkcu_poly_job *jobs, int njobs,
-		const vkcu_poly_job *one, uint32_t log_n, int sms);
+		const vkcu_poly_job *one, uint32_t log_n, int wide, int sms);
 /* The same with an epilogue (`lift` NULL or count 0: none); fused into the
  * last pass for 2^8 <= n <= 2^17, a separate element-wise launch otherwise. */
 int vkcu_ntt_inverse_lift(void *stream, const vkcu_ntt_job *jobs, int njobs,
-		const vkcu_ntt_job *one, uint32_t log_n, int sms, const vkcu_lift *lift);
+		const vkcu_ntt_job *one, uint32_t log_n, int wide, int sms, const vkcu_lift *lift);
 int vkcu_polymul_lift(void *stream, const vkcu_poly_job *jobs, int njobs,
-		const vkcu_poly_job *one, uint32_t log_n, int sms, const vkcu_lift *lift);
+		const vkcu_poly_job *one, uint32_t log_n, int wide, int sms, const vkcu_lift *lift);
 /* The epilogue alone, in place on `len` words at p (modulus q for TABLE_Q
  * steps), or on the n output words of every job. */
 int vkcu_lift_range(void *stream, uint64_t *p, uint64_t len, uint64_t q, const vkcu_lift *lift);
 int vkcu_lift_jobs(void *stream, const vkcu_ntt_job *jobs, int njobs, const vkcu_ntt_job *one,
 		uint32_t log_n, int sms, const vkcu_lift *lift);
-/* c = c * scratch mod q (lazy inputs from the forward transforms, canonical
- * output) for every job: the pointwise step of a polymul that is not fused. */
+/* c = c * scratch mod q for every job (both canonical forward-transform
+ * outputs; the word the reference's elemmul stores): the pointwise step of a
+ * polymul that is not fused. */
 int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,
-		uint32_t log_n, int sms);
+		uint32_t log_n, int wide, int sms);
 /* Kernel variant table (tuning.c): family 0 = fused polymul, 1 = forward,
  * 2 = inverse, 3 = batch options. */
 int vkh_variant(int family, int log_n);
 /* Integer-pipe microbenchmarks (peak.cu). */
 int vkcu_measure_int_peak(void *stream, int sms, double *bfly_per_s, double *imad_per_s);
 /* Largest log_n of the single-launch kernels (one CTA up to 2^14, one
- * cluster up to 2^17), and the largest log_n handled at all (2^18). */
+ * cluster up to 2^17), and the largest log_n handled at all (2^26: passes
+ * over HBM plus 2^14-word sub-blocks). */
 uint32_t vkcu_max_fused_log_n(void);
 uint32_t vkcu_max_log_n(void);
 

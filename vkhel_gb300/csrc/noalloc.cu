@@ -77,8 +77,8 @@ extern "C" VKHEL_EXPORT int vkhel_vector_polymul_noalloc(const struct vkhel_vect
     return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED,
                     "polymul_noalloc: n=%llu outside 256..%llu (static scratch of %llu words)",
                     (unsigned long long)t->n, kNoallocMaxWords, kNoallocMaxWords);
-  if (t->q < 3 || t->q >= (1ull << 62))
-    return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "polymul_noalloc: q outside [3, 2^62)");
+  if (t->q < 3 || t->q >= (1ull << 63) || t->unreduced)
+    return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "polymul_noalloc: q outside [3, 2^63) or tables not reduced");
   if (a->length < t->n || b->length < t->n || result->length < t->n)
     return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "polymul_noalloc: vectors shorter than n");
   const struct vkh_devtab* d = vkh_devtab_find(ctx, t);
@@ -90,7 +90,7 @@ extern "C" VKHEL_EXPORT int vkhel_vector_polymul_noalloc(const struct vkhel_vect
   int e = scratch_address(ctx->device, &scratch);
   if (e) return vkh_cuda(ctx, e, "polymul_noalloc: scratch address");
   const vkcu_poly_job job = {a->dev, b->dev, result->dev, static_cast<uint64_t*>(scratch), d->dev_set};
-  e = vkcu_polymul(ctx->stream, nullptr, 1, &job, t->log_n, ctx->sms);
+  e = vkcu_polymul(ctx->stream, nullptr, 1, &job, t->log_n, vkcu_wide(t->q), ctx->sms);
   if (!e) e = vkcu_sync(ctx->stream);
   return vkh_cuda(ctx, e, "polymul_noalloc");
 }

@@ -1,7 +1,8 @@
 // Transform dispatch and the kernels outside the CTA-resident families:
 // simple one-stage-per-barrier kernels (n < 256, unaligned operands), the
-// global-memory head/tail passes of n > 2^14, and the pointwise step of a
-// composed polynomial multiply.  The CTA-resident kernels are in
+// global-memory passes of n >= 2^18, and the pointwise step of a composed
+// polynomial multiply.  Every launcher takes the modulus class of its jobs
+// (`wide`: 2^62 <= q < 2^63).  The CTA-resident kernels are in
 // ntt_core.cuh with one launcher per family (ntt_fwd.cu, ntt_inv.cu,
 // ntt_poly.cu).
 #include "ntt_core.cuh"
@@ -13,6 +14,7 @@ namespace vk {
 // radix-2 stage per __syncthreads.  Used for n < 256, for n <= 2^14 when a
 // pointer is not 32-byte aligned, and as an independent cross-check.
 
+template <class M>
 __global__ void k_ntt_fwd_simple(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
                                  int log_n) {
   extern __shared__ u64 sm[];
@@ -30,18 +32,19 @@ __global__ void k_ntt_fwd_simple(const vkcu_ntt_job* __restrict__ jobs, int njob
         const int x = blk * 2 * half + (p & (half - 1));
         const ulonglong2 wt = ld_tw(t.fwd + (1 << s) + blk);
         if (s == 0)
-          ct_first(sm[x], sm[x + half], wt.x, wt.y, t);
+          ct_first<M>(sm[x], sm[x + half], wt.x, wt.y, t);
         else
-          ct_bfly(sm[x], sm[x + half], wt.x, wt.y, t.q, t.q2);
+          M::ct(sm[x], sm[x + half], wt.x, wt.y, t);
       }
       __syncthreads();
     }
     u64* out = reinterpret_cast<u64*>(job.out);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = canon4(sm[i], t.q, t.q2);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = M::canon(sm[i], t);
     __syncthreads();
   }
 }
 
+template <class M>
 __global__ void k_ntt_inv_simple(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
                                  int log_n) {
   extern __shared__ u64 sm[];
@@ -58,12 +61,10 @@ __global__ void k_ntt_inv_simple(const vkcu_ntt_job* __restrict__ jobs, int njob
         const int blk = p >> (log_n - 1 - s);
         const int x = blk * 2 * half + (p & (half - 1));
         u64 sum, dif;
-        if (s == log_n - 1) {
-          gs_first_sd(sm[x], sm[x + half], t, sum, dif);
-        } else {
-          sum = sm[x] + sm[x + half];
-          dif = sm[x] - sm[x + half] + t.q2;
-        }
+        if (s == log_n - 1)
+          gs_first_sd<M>(sm[x], sm[x + half], t, sum, dif);
+        else
+          M::sd(sm[x], sm[x + half], t, sum, dif);
         if (s == 0) {
           sm[x] = shoup(sum, t.ninv, t.ninv_s, t.q);
           sm[x + half] = shoup(dif, t.w1ninv, t.w1ninv_s, t.q);
@@ -82,66 +83,93 @@ __global__ void k_ntt_inv_simple(const vkcu_ntt_job* __restrict__ jobs, int njob
 }
 
 // ---------------------------------------------------------------------------
-// Global-memory passes for n > 2^14 (KK = log2(n) - 14 stages, KK <= 4).
-// Forward: global stages 0 .. KK-1, in -> out, lazy [0, 2q).  Each thread
-// owns one group of 2^KK words at stride n / 2^KK (coalesced).
-template <int KK>
-__global__ void k_fwd_head_global(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
-                                  int log_n) {
-  const int groups = 1 << (log_n - KK);
+// Global-memory passes for n >= 2^18: the first (forward) or last (inverse)
+// log2(n) - 14 stages run over HBM in passes of KK <= 4 stages each, and
+// one CTA-resident kernel runs the other 14 stages on every 2^14-word
+// sub-block (sub-block r uses twiddle multiplier 2^(log2 n - 14) + r).  A
+// pass starting at stage s0 gives each thread one radix-2^KK group: the
+// 2^KK words at stride t = n >> (s0 + KK) inside one block of stage s0
+// (blocks of n >> s0 words), twiddle base 2^s0 + block (root index m + block
+// of the reference's stage loop, src/vector.c:536-566).  Consecutive threads
+// take consecutive offsets, so every load and store is coalesced.
+
+// Forward: stages s0 .. s0 + KK - 1, in -> out, forward-lazy; stage 0 takes
+// the reference's exact first-stage rule; the last pass (handoff) leaves
+// words below the sub-block kernels' first-stage fast-path bound.
+template <int KK, class M>
+__global__ void k_fwd_global(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int log_n, int s0,
+                             int handoff) {
+  const int lt = log_n - s0 - KK;  // log2 of the stride
+  const long groups = 1L << (log_n - KK);
   const long total = (long)njobs * groups;
   for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < total; w += (long)gridDim.x * blockDim.x) {
-    const vkcu_ntt_job job = fetch_job(jobs, one, (int)(w / groups));
-    const int o = (int)(w % groups);
+    const vkcu_ntt_job job = fetch_job(jobs, one, (int)(w >> (log_n - KK)));
+    const long g = w & (groups - 1);
+    const long blk = g >> lt;
+    const size_t first = ((size_t)blk << (log_n - s0)) | (size_t)(g & ((1L << lt) - 1));
+    const size_t st = (size_t)1 << lt;
     const Tw t = load_tw(job.tw);
-    const u64* in = reinterpret_cast<const u64*>(job.in);
+    const u64* in = reinterpret_cast<const u64*>(s0 ? job.out : job.in);
     u64 v[1 << KK];
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[j] = ld_stream(in + o + (size_t)j * groups);
-    const ulonglong2 w0 = ld_tw(t.fwd + 1);
+    for (int j = 0; j < (1 << KK); j++) v[j] = ld_stream(in + first + j * st);
+    const u32 base = (1u << s0) + (u32)blk;
+    if (s0 == 0) {
+      const ulonglong2 w0 = ld_tw(t.fwd + 1);
 #pragma unroll
-    for (int jj = 0; jj < (1 << (KK - 1)); jj++) ct_first(v[jj], v[jj + (1 << (KK - 1))], w0.x, w0.y, t);
-    ct_group<KK, 1, 0>(v, t.fwd, 1u, t);
+      for (int jj = 0; jj < (1 << (KK - 1)); jj++) ct_first<M>(v[jj], v[jj + (1 << (KK - 1))], w0.x, w0.y, t);
+      ct_group<M, KK, 1, 0>(v, t.fwd, base, t);
+    } else {
+      ct_group<M, KK, 0, 0>(v, t.fwd, base, t);
+    }
     u64* out = reinterpret_cast<u64*>(job.out);
-    // below 2q, so the sub-block kernels' first stage stays on its fast path
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) out[o + (size_t)j * groups] = csub(v[j], t.q2);
+    for (int j = 0; j < (1 << KK); j++) out[first + j * st] = handoff ? M::handoff(v[j], t) : v[j];
   }
 }
 
-// Inverse: global stages KK-1 .. 0 on `out` in place (after the sub-block
-// kernels), with n^-1 folded in, canonical output.
-template <int KK>
-__global__ void k_inv_tail_global(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
-                                  int log_n) {
-  const int groups = 1 << (log_n - KK);
+// Inverse: stages s0 + KK - 1 .. s0 on `out` in place (after the sub-block
+// kernels, which leave inverse-lazy words); the pass with s0 = 0 folds n^-1
+// into stage 0 and writes canonical words.
+template <int KK, class M>
+__global__ void k_inv_global(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int log_n, int s0) {
+  const int lt = log_n - s0 - KK;
+  const long groups = 1L << (log_n - KK);
   const long total = (long)njobs * groups;
   for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < total; w += (long)gridDim.x * blockDim.x) {
-    const vkcu_ntt_job job = fetch_job(jobs, one, (int)(w / groups));
-    const int o = (int)(w % groups);
+    const vkcu_ntt_job job = fetch_job(jobs, one, (int)(w >> (log_n - KK)));
+    const long g = w & (groups - 1);
+    const long blk = g >> lt;
+    const size_t first = ((size_t)blk << (log_n - s0)) | (size_t)(g & ((1L << lt) - 1));
+    const size_t st = (size_t)1 << lt;
     const Tw t = load_tw(job.tw);
     u64* out = reinterpret_cast<u64*>(job.out);
     u64 v[1 << KK];
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) v[j] = out[o + (size_t)j * groups];
-    gs_group<KK, 0, false, true>(v, t.inv, 1u, t);
+    for (int j = 0; j < (1 << KK); j++) v[j] = out[first + j * st];
+    const u32 base = (1u << s0) + (u32)blk;
+    if (s0 == 0)
+      gs_group<M, KK, 0, false, true>(v, t.inv, base, t);
+    else
+      gs_group<M, KK, 0, false, false>(v, t.inv, base, t);
 #pragma unroll
-    for (int j = 0; j < (1 << KK); j++) out[o + (size_t)j * groups] = v[j];
+    for (int j = 0; j < (1 << KK); j++) out[first + j * st] = v[j];
   }
 }
 
 static constexpr int kMaxCta = 14;      // one CTA per transform
 static constexpr int kMaxCluster = 17;  // one cluster of up to 8 CTAs
-static constexpr int kMaxLogN = 18;     // one global pass + 2^14 sub-blocks
+static constexpr int kMaxLogN = 26;     // global passes + 2^14-word sub-blocks
 
 static bool aligned32(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31) == 0; }
 
+template <class M>
 static int simple(cudaStream_t st, bool inverse, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one,
                   int log_n, int sms) {
   const int n = 1 << log_n;
   const int threads = n / 2 < 32 ? 32 : (n / 2 > 512 ? 512 : n / 2);
   const int smem = n * 8;
-  auto kern = inverse ? k_ntt_inv_simple : k_ntt_fwd_simple;
+  auto kern = inverse ? k_ntt_inv_simple<M> : k_ntt_fwd_simple<M>;
   // threads and shared memory depend on n: one occupancy per direction and
   // degree; the kernel's shared-memory limit is the largest n (2^14) always
   static KernelSetup setups[2][kMaxCta + 1];
@@ -153,21 +181,31 @@ static int simple(cudaStream_t st, bool inverse, const vkcu_ntt_job* jobs, int n
   return (int)cudaGetLastError();
 }
 
-template <bool INV>
-static int global_pass(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n,
-                       int kk, int sms) {
+// Stages of the global pass p (0-based, in forward order) for log_n: the
+// log_n - 14 global stages split into as few passes of <= 4 stages as
+// possible, sizes as equal as possible (2^21: 4 + 3).
+static int global_passes(int log_n) { return (log_n - kMaxCta + 3) / 4; }
+static void global_split(int log_n, int p, int* s0, int* kk) {
+  const int g = log_n - kMaxCta, np = global_passes(log_n), small = g / np, big = g % np;
+  *s0 = p * small + (p < big ? p : big);
+  *kk = small + (p < big ? 1 : 0);
+}
+
+template <class M>
+static int global_pass(cudaStream_t st, bool inverse, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one,
+                       int log_n, int s0, int kk, int handoff, int sms) {
   const long work = (long)njobs << (log_n - kk);
   const int threads = 256;
   long blocks = (work + threads - 1) / threads;
   const long cap = (long)sms * 8;
   if (blocks > cap) blocks = cap;
   switch (kk) {
-#define G(K)                                                                                \
-  case K:                                                                                   \
-    if (INV)                                                                                \
-      k_inv_tail_global<K><<<(int)blocks, threads, 0, st>>>(jobs, njobs, one, log_n);       \
-    else                                                                                    \
-      k_fwd_head_global<K><<<(int)blocks, threads, 0, st>>>(jobs, njobs, one, log_n);       \
+#define G(K)                                                                                          \
+  case K:                                                                                             \
+    if (inverse)                                                                                      \
+      k_inv_global<K, M><<<(int)blocks, threads, 0, st>>>(jobs, njobs, one, log_n, s0);               \
+    else                                                                                              \
+      k_fwd_global<K, M><<<(int)blocks, threads, 0, st>>>(jobs, njobs, one, log_n, s0, handoff);      \
     break;
     G(1)
     G(2)
@@ -203,47 +241,74 @@ static bool split_small(int njobs, uint32_t log_n, int sms) {
 }
 
 extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
-                                uint32_t log_n, int sms) {
+                                uint32_t log_n, int wide, int sms) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
   if (log_n < 1 || log_n > (uint32_t)kMaxLogN || njobs < 1) return (int)cudaErrorInvalidValue;
   const bool aligned = jobs_aligned(jobs, one);
-  if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) return simple(st, false, jobs, njobs, o, (int)log_n, sms);
+  if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned))
+    return wide ? simple<Mod63>(st, false, jobs, njobs, o, (int)log_n, sms)
+                : simple<Mod62>(st, false, jobs, njobs, o, (int)log_n, sms);
   if (!aligned) return (int)cudaErrorMisalignedAddress;
-  if (split_small(njobs, log_n, sms)) return fwd_cluster(st, jobs, njobs, o, 3, (int)log_n - 3);
-  if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(1, (int)log_n));
-  if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta);
-  const int kk = (int)log_n - kMaxCta;
-  if (int e = global_pass<false>(st, jobs, njobs, o, (int)log_n, kk, sms)) return e;
-  return fwd_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(1, kMaxCta));
+  if (wide) {
+    if (log_n <= (uint32_t)kMaxCta) return fwd_cta_wide(st, jobs, njobs, o, (int)log_n, 0, sms);
+    if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta);
+  } else {
+    if (split_small(njobs, log_n, sms)) return fwd_cluster(st, jobs, njobs, o, 3, (int)log_n - 3);
+    if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(1, (int)log_n));
+    if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta);
+  }
+  const int np = global_passes((int)log_n);
+  for (int p = 0; p < np; p++) {
+    int s0, kk;
+    global_split((int)log_n, p, &s0, &kk);
+    const int e = wide ? global_pass<Mod63>(st, false, jobs, njobs, o, (int)log_n, s0, kk, p == np - 1, sms)
+                       : global_pass<Mod62>(st, false, jobs, njobs, o, (int)log_n, s0, kk, p == np - 1, sms);
+    if (e) return e;
+  }
+  const int sub_log = (int)log_n - kMaxCta;
+  return wide ? fwd_cta_wide(st, jobs, njobs, o, kMaxCta, sub_log, sms)
+              : fwd_cta(st, jobs, njobs, o, kMaxCta, sub_log, sms, vkh_variant(1, kMaxCta));
 }
 
 static bool has_lift(const vkcu_lift* lift) { return lift && lift->count > 0; }
 
 extern "C" int vkcu_ntt_inverse_lift(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
-                                     uint32_t log_n, int sms, const vkcu_lift* lift) {
+                                     uint32_t log_n, int wide, int sms, const vkcu_lift* lift) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
   if (log_n < 1 || log_n > (uint32_t)kMaxLogN || njobs < 1) return (int)cudaErrorInvalidValue;
   if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
   const bool aligned = jobs_aligned(jobs, one);
   const bool lifted = has_lift(lift);
+  const vkcu_lift* lp = lifted ? lift : nullptr;
   int e;
   if (log_n < 8 || (log_n <= (uint32_t)kMaxCta && !aligned)) {
-    e = simple(st, true, jobs, njobs, o, (int)log_n, sms);
+    e = wide ? simple<Mod63>(st, true, jobs, njobs, o, (int)log_n, sms)
+             : simple<Mod62>(st, true, jobs, njobs, o, (int)log_n, sms);
   } else if (!aligned) {
     return (int)cudaErrorMisalignedAddress;
-  } else if (split_small(njobs, log_n, sms)) {
-    return inv_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lifted ? lift : nullptr);
-  } else if (log_n <= (uint32_t)kMaxCta) {
+  } else if (wide && log_n <= (uint32_t)kMaxCta) {
+    return inv_cta_wide(st, jobs, njobs, o, (int)log_n, 0, sms, lp);
+  } else if (wide && log_n <= (uint32_t)kMaxCluster) {
+    return inv_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta, lp);
+  } else if (!wide && split_small(njobs, log_n, sms)) {
+    return inv_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
+  } else if (!wide && log_n <= (uint32_t)kMaxCta) {
     if (lifted) return inv_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
     return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(2, (int)log_n));
-  } else if (log_n <= (uint32_t)kMaxCluster) {
-    return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lifted ? lift : nullptr);
+  } else if (!wide && log_n <= (uint32_t)kMaxCluster) {
+    return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lp);
   } else {
-    const int kk = (int)log_n - kMaxCta;
-    e = inv_cta(st, jobs, njobs, o, kMaxCta, kk, sms, vkh_variant(2, kMaxCta));
-    if (!e) e = global_pass<true>(st, jobs, njobs, o, (int)log_n, kk, sms);
+    const int sub_log = (int)log_n - kMaxCta;
+    e = wide ? inv_cta_wide(st, jobs, njobs, o, kMaxCta, sub_log, sms, nullptr)
+             : inv_cta(st, jobs, njobs, o, kMaxCta, sub_log, sms, vkh_variant(2, kMaxCta));
+    for (int p = global_passes((int)log_n) - 1; !e && p >= 0; p--) {
+      int s0, kk;
+      global_split((int)log_n, p, &s0, &kk);
+      e = wide ? global_pass<Mod63>(st, true, jobs, njobs, o, (int)log_n, s0, kk, 0, sms)
+               : global_pass<Mod62>(st, true, jobs, njobs, o, (int)log_n, s0, kk, 0, sms);
+    }
   }
   // the multi-launch paths take the epilogue as one more element-wise launch
   if (!e && lifted) e = vkcu_lift_jobs(stream, jobs, njobs, one, log_n, sms, lift);
@@ -251,27 +316,32 @@ extern "C" int vkcu_ntt_inverse_lift(void* stream, const vkcu_ntt_job* jobs, int
 }
 
 extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
-                                uint32_t log_n, int sms) {
-  return vkcu_ntt_inverse_lift(stream, jobs, njobs, one, log_n, sms, nullptr);
+                                uint32_t log_n, int wide, int sms) {
+  return vkcu_ntt_inverse_lift(stream, jobs, njobs, one, log_n, wide, sms, nullptr);
 }
 
 extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,
-                                 uint32_t log_n, int sms, const vkcu_lift* lift) {
+                                 uint32_t log_n, int wide, int sms, const vkcu_lift* lift) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
   if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
   if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
-  if (split_small(njobs, log_n, sms)) return poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, has_lift(lift) ? lift : nullptr);
+  const vkcu_lift* lp = has_lift(lift) ? lift : nullptr;
+  if (wide) {
+    if (log_n <= (uint32_t)kMaxCta) return poly_cta_wide(st, jobs, njobs, o, (int)log_n, sms, lp);
+    return poly_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta, lp);
+  }
+  if (split_small(njobs, log_n, sms)) return poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
   if (log_n <= (uint32_t)kMaxCta) {
-    if (has_lift(lift)) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n), *lift);
+    if (lp) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n), *lift);
     return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
   }
-  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, has_lift(lift) ? lift : nullptr);
+  return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lp);
 }
 
 extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,
-                            uint32_t log_n, int sms) {
-  return vkcu_polymul_lift(stream, jobs, njobs, one, log_n, sms, nullptr);
+                            uint32_t log_n, int wide, int sms) {
+  return vkcu_polymul_lift(stream, jobs, njobs, one, log_n, wide, sms, nullptr);
 }
 
 // The epilogue as its own element-wise pass: over `len` words at p, or over
@@ -324,7 +394,9 @@ extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs,
 }
 
 // Pointwise step of a composed polymul: c = c * scratch mod q over njobs
-// jobs of n words each (both operands canonical NTT outputs).
+// jobs of n words each (both operands canonical NTT outputs), the word the
+// reference's elemmul stores.
+template <class M>
 __global__ void k_pointwise(const vkcu_poly_job* __restrict__ jobs, int njobs, int log_n) {
   const long n = 1L << log_n;
   const long total = (long)njobs * n;
@@ -334,16 +406,19 @@ __global__ void k_pointwise(const vkcu_poly_job* __restrict__ jobs, int njobs, i
     const Tw t = load_tw(job.tw);
     u64* c = reinterpret_cast<u64*>(job.c);
     const u64 x = c[i], y = reinterpret_cast<const u64*>(job.scratch)[i];
-    c[i] = csub(barrett_mul_lazy(x, y, t.q, t.q2, t.mu, t.qbits), t.q);
+    c[i] = M::product_out(x, y, t);
   }
 }
 
-extern "C" int vkcu_pointwise(void* stream, const vkcu_poly_job* jobs, int njobs, uint32_t log_n, int sms) {
+extern "C" int vkcu_pointwise(void* stream, const vkcu_poly_job* jobs, int njobs, uint32_t log_n, int wide, int sms) {
   if (njobs < 1 || !jobs) return (int)cudaErrorInvalidValue;
   const long work = (long)njobs << log_n;
   long blocks = (work + 255) / 256;
   if (blocks > (long)sms * 8) blocks = (long)sms * 8;
-  k_pointwise<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, (int)log_n);
+  if (wide)
+    k_pointwise<Mod63><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, (int)log_n);
+  else
+    k_pointwise<Mod62><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, (int)log_n);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
 }

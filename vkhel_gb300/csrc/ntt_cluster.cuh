@@ -38,6 +38,7 @@ namespace cg = cooperative_groups;
 namespace vk {
 
 using SubShape = Shape<14, 32>;  // the large-n sub-block
+using SubShape63 = Shape<14, 32, 1, Mod63>;  // the same for 2^62 <= q < 2^63
 
 template <int LOGC, class S>
 struct Cols {
@@ -56,7 +57,7 @@ __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
 // Forward column pass: global stages 0 .. LOGC-1 (exact first-stage rule),
-// outputs scattered to the owning CTAs' shared memory, lazy [0, 4q).  A
+// outputs scattered to the owning CTAs' shared memory, forward-lazy.  A
 // thread's PER columns go in two rounds of H = PER / 2 (16 words in flight:
 // all 32 at once would spill).  SPLIT: the caller has arrived on the cluster
 // barrier that frees the other CTAs' shared memory, and the first round's
@@ -79,8 +80,9 @@ __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, con
     static_for<0, H>([&](auto kc) {
       constexpr int k = decltype(kc)::value;
 #pragma unroll
-      for (int jj = 0; jj < K::C / 2; jj++) ct_first(v[k * K::C + jj], v[k * K::C + jj + K::C / 2], w0.x, w0.y, t);
-      ct_group<LOGC, 1, k * K::C>(v, t.fwd, 1u, t);
+      for (int jj = 0; jj < K::C / 2; jj++)
+        ct_first<typename S::M>(v[k * K::C + jj], v[k * K::C + jj + K::C / 2], w0.x, w0.y, t);
+      ct_group<typename S::M, LOGC, 1, k * K::C>(v, t.fwd, 1u, t);
     });
     if (SPLIT && k0 == 0) cluster_wait();
 #pragma unroll
@@ -110,7 +112,7 @@ __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg
     }
     static_for<0, H>([&](auto kc) {
       constexpr int k = decltype(kc)::value;
-      gs_group<LOGC, k * K::C, false, true>(v, t.inv, 1u, t);
+      gs_group<typename S::M, LOGC, k * K::C, false, true>(v, t.inv, 1u, t);
     });
 #pragma unroll
     for (int k = 0; k < H; k++)
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(S::T, 1)
     fwd_first_smem<S>(sm, t, tw_mult);
     fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
 #pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+      for (int j = 0; j < 16; j++) v[j] = S::M::canon(v[j], t);
       store16(v, out + 16 * g);
     });
   }
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(S::T, 1)
       const int g = (int)threadIdx.x + i * S::T;
       u64 v[16];
       load16(v, in + 16 * g);
-      gs_group<4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+      gs_group<typename S::M, 4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
 #pragma unroll
       for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
     }
@@ -214,17 +216,18 @@ __global__ void __launch_bounds__(S::T, 1)
       cl.sync();
       fwd_first_smem<S>(sm, t, tw_mult);
       fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
+        using M = typename S::M;
         if (ph == 0) {
 #pragma unroll
-          for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+          for (int j = 0; j < 16; j++) v[j] = M::canon(v[j], t);
           store16(v, scratch + 16 * g);
         } else {
           u64 bh[16];
           load16(bh, scratch + 16 * g);
 #pragma unroll
-          for (int j = 0; j < 16; j++) v[j] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+          for (int j = 0; j < 16; j++) v[j] = M::product(v[j], bh[j], t);
           // the sub-block's first inverse pass (stages HEAD + 3 .. HEAD) on the same words
-          gs_group<4, 0, false, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+          gs_group<M, 4, 0, M::EXACT_AFTER_PRODUCT, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
 #pragma unroll
           for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
         }

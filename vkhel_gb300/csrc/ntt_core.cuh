@@ -26,7 +26,10 @@
 //   * the last inverse pass folds n^-1 into its final stage and writes global
 //     memory coalesced.
 // Butterflies are lazy (Harvey): values stay in [0, 4q) (forward) or [0, 2q)
-// (inverse) and are made canonical once at the end.
+// (inverse) and are made canonical once at the end.  That needs 4q <= 2^64;
+// moduli 2^62 <= q < 2^63 (the top of the reference's range: its inverse-mod
+// works below 2^63, src/numbers.c:71-99) run the same kernels instantiated
+// with the Mod63 class below, whose values stay in [0, 2q) both ways.
 //
 // Bit-exactness for unreduced inputs.  The reference's first stage computes
 // (X + WY) mod 2^64 mod q and (X - WY) mod q (forward), or (X + Y) mod 2^64
@@ -112,38 +115,142 @@ struct U2 {
 
 // The reference's stage-0 butterfly for x >= 2q, exactly: X' = (X + WY) mod
 // 2^64 mod q, Y' = (X - WY) mod q.  Kept out of line: it is rarely taken.
+// reduce64 is an exact remainder for q < 2^62.
 static __device__ __noinline__ U2 ct_first_slow(u64 x, u64 y, u64 w, u64 wp, u64 q, u64 mu, u32 qbits) {
   const u64 wy = shoup(y, w, wp, q);
   const u64 xr = ref_reduce64(x, q, mu, qbits);
   return U2{ref_reduce64(x + wy, q, mu, qbits), xr >= wy ? xr - wy : xr + q - wy};
 }
 
-// Forward, stage m = 1.  Fast path whenever x < 2q: then x + WY < 3q < 2^64,
-// so the reference does not wrap and the lazy result is congruent.
-__device__ __forceinline__ void ct_first(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
-  if (x < t.q2) {
-    ct_bfly(x, y, w, wp, t.q, t.q2);
-  } else {
-    const U2 r = ct_first_slow(x, y, w, wp, t.q, t.mu, t.qbits);
-    x = r.x;
-    y = r.y;
-  }
-}
-
 // Inverse, stage m = n/2: the sum s and difference d before the twiddle
-// product; s in [0, 4q), d in (0, 4q).
+// product, exactly as the reference's (X + Y) mod 2^64 mod q and the
+// residue of its `while (t < Y) t += q; t -= Y` loop.
 static __device__ __noinline__ U2 gs_first_slow(u64 x, u64 y, u64 q, u64 mu, u32 qbits) {
   const u64 xr = ref_reduce64(x, q, mu, qbits);
   const u64 yr = ref_reduce64(y, q, mu, qbits);
   return U2{ref_reduce64(x + y, q, mu, qbits), xr >= yr ? xr - yr : xr + q - yr};
 }
 
-__device__ __forceinline__ void gs_first_sd(u64 x, u64 y, const Tw& t, u64& s, u64& d) {
-  if (x < t.q2 && y < t.q2) {
+// The same two for 2^62 <= q < 2^63, with the exact 64-bit remainder.
+static __device__ __noinline__ U2 ct_first_slow63(u64 x, u64 y, u64 w, u64 wp, u64 q) {
+  const u64 wy = shoup(y, w, wp, q);
+  const u64 xr = x % q;
+  return U2{(x + wy) % q, xr >= wy ? xr - wy : xr + q - wy};
+}
+
+static __device__ __noinline__ U2 gs_first_slow63(u64 x, u64 y, u64 q) {
+  const u64 xr = x % q, yr = y % q;
+  return U2{(x + y) % q, xr >= yr ? xr - yr : xr + q - yr};
+}
+
+// ---------------------------------------------------------------------------
+// Modulus classes: the butterfly arithmetic every kernel is instantiated with.
+//
+// Mod62 (q < 2^62): forward values in [0, 4q), inverse values in [0, 2q), one
+// conditional subtraction per butterfly (Harvey).  The pointwise product is
+// a Barrett product whose result is congruent to the reference's elemmul
+// (exact for these moduli).
+//
+// Mod63 (2^62 <= q < 2^63, where 4q overflows): forward and inverse values in
+// [0, 2q), two conditional subtractions per butterfly.  The pointwise
+// product restates the reference's elemmul formula word for word
+// (elemmul.comp:49-73): with a 63-bit modulus its Barrett estimate
+// (hi << 3) + (lo >> 61) wraps past 2^64 for large products, so its results
+// are not the true residues, and the polymul must reproduce them; the
+// inverse stage that follows then takes the exact first-stage rule, since
+// such a word need not be below q.
+struct Mod62 {
+  static constexpr bool EXACT_AFTER_PRODUCT = false;
+  __device__ __forceinline__ static void ct(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
+    ct_bfly(x, y, w, wp, t.q, t.q2);
+  }
+  __device__ __forceinline__ static void gs(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
+    gs_bfly(x, y, w, wp, t.q, t.q2);
+  }
+  // sum and difference of two inverse-lazy words before the twiddle product
+  __device__ __forceinline__ static void sd(u64 x, u64 y, const Tw& t, u64& s, u64& d) {
     s = x + y;
     d = x - y + t.q2;
+  }
+  // forward-lazy word -> canonical
+  __device__ __forceinline__ static u64 canon(u64 x, const Tw& t) { return canon4(x, t.q, t.q2); }
+  // forward-lazy word -> below the next kernel's first-stage fast-path bound
+  __device__ __forceinline__ static u64 handoff(u64 x, const Tw& t) { return csub(x, t.q2); }
+  // first-stage fast paths: the lazy butterfly is congruent to the reference's
+  __device__ __forceinline__ static bool fwd_fast(u64 x, const Tw& t) { return x < t.q2; }
+  __device__ __forceinline__ static bool inv_fast(u64 x, u64 y, const Tw& t) { return x < t.q2 && y < t.q2; }
+  __device__ __forceinline__ static U2 ct_slow(u64 x, u64 y, u64 w, u64 wp, const Tw& t) {
+    return ct_first_slow(x, y, w, wp, t.q, t.mu, t.qbits);
+  }
+  __device__ __forceinline__ static U2 gs_slow(u64 x, u64 y, const Tw& t) {
+    return gs_first_slow(x, y, t.q, t.mu, t.qbits);
+  }
+  // pointwise product of a forward-lazy word and a canonical one: an
+  // inverse-lazy word (fused kernels) ...
+  __device__ __forceinline__ static u64 product(u64 x, u64 y, const Tw& t) {
+    return barrett_mul_lazy(canon4(x, t.q, t.q2), y, t.q, t.q2, t.mu, t.qbits);
+  }
+  // ... or, from two canonical words, the word the reference's elemmul stores
+  __device__ __forceinline__ static u64 product_out(u64 x, u64 y, const Tw& t) {
+    return csub(barrett_mul_lazy(x, y, t.q, t.q2, t.mu, t.qbits), t.q);
+  }
+};
+
+struct Mod63 {
+  static constexpr bool EXACT_AFTER_PRODUCT = true;
+  __device__ __forceinline__ static void ct(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
+    const u64 xr = csub(x, t.q);
+    const u64 wy = csub(shoup_lazy(y, w, wp, t.q), t.q);
+    x = xr + wy;
+    y = xr - wy + t.q;
+  }
+  __device__ __forceinline__ static void sd(u64 x, u64 y, const Tw& t, u64& s, u64& d) {
+    const u64 xr = csub(x, t.q), yr = csub(y, t.q);
+    s = xr + yr;
+    d = xr - yr + t.q;
+  }
+  __device__ __forceinline__ static void gs(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
+    u64 s, d;
+    sd(x, y, t, s, d);
+    x = s;
+    y = shoup_lazy(d, w, wp, t.q);
+  }
+  __device__ __forceinline__ static u64 canon(u64 x, const Tw& t) { return csub(x, t.q); }
+  __device__ __forceinline__ static u64 handoff(u64 x, const Tw& t) { return csub(x, t.q); }
+  __device__ __forceinline__ static bool fwd_fast(u64 x, const Tw& t) { return x < t.q; }
+  __device__ __forceinline__ static bool inv_fast(u64 x, u64 y, const Tw& t) { return x < t.q && y < t.q; }
+  __device__ __forceinline__ static U2 ct_slow(u64 x, u64 y, u64 w, u64 wp, const Tw& t) {
+    return ct_first_slow63(x, y, w, wp, t.q);
+  }
+  __device__ __forceinline__ static U2 gs_slow(u64 x, u64 y, const Tw& t) { return gs_first_slow63(x, y, t.q); }
+  // the reference's elemmul on canonical operands (its reduce64 returns them
+  // unchanged): the full 128-bit product through reduce128
+  __device__ __forceinline__ static u64 product_out(u64 x, u64 y, const Tw& t) {
+    return ref_reduce128(mulhi(x, y), x * y, t.q, t.mu, t.qbits);
+  }
+  __device__ __forceinline__ static u64 product(u64 x, u64 y, const Tw& t) { return product_out(csub(x, t.q), y, t); }
+};
+
+// Forward, stage m = 1, with the reference's exact rule for inputs outside
+// the fast path (x >= 2q for Mod62: then x + WY < 3q < 2^64 no longer holds).
+template <class M>
+__device__ __forceinline__ void ct_first(u64& x, u64& y, u64 w, u64 wp, const Tw& t) {
+  if (M::fwd_fast(x, t)) {
+    M::ct(x, y, w, wp, t);
   } else {
-    const U2 r = gs_first_slow(x, y, t.q, t.mu, t.qbits);
+    const U2 r = M::ct_slow(x, y, w, wp, t);
+    x = r.x;
+    y = r.y;
+  }
+}
+
+// Inverse, stage m = n/2: s and d with the exact rule outside the fast path.
+template <class M>
+__device__ __forceinline__ void gs_first_sd(u64 x, u64 y, const Tw& t, u64& s, u64& d) {
+  if (M::inv_fast(x, y, t)) {
+    M::sd(x, y, t, s, d);
+  } else {
+    const U2 r = M::gs_slow(x, y, t);
     s = r.x;
     d = r.y;
   }
@@ -155,7 +262,7 @@ __device__ __forceinline__ void gs_first_sd(u64 x, u64 y, const Tw& t, u64& s, u
 // of the pass; `base` = (tw_mult * m0 + block) so that the root of sub-stage u
 // and sub-block r is table[(base << u) + r].
 
-template <int KK, int U0, int G0, int NV>
+template <class M, int KK, int U0, int G0, int NV>
 __device__ __forceinline__ void ct_group(u64 (&v)[NV], const ulonglong2* tw, u32 base, const Tw& t) {
   static_for<U0, KK>([&](auto uc) {
     constexpr int u = decltype(uc)::value;
@@ -165,7 +272,7 @@ __device__ __forceinline__ void ct_group(u64 (&v)[NV], const ulonglong2* tw, u32
       const ulonglong2 w = ld_tw(tw + ((base << u) + r));
 #pragma unroll
       for (int jj = 0; jj < half; jj++)
-        ct_bfly(v[G0 + r * 2 * half + jj], v[G0 + r * 2 * half + jj + half], w.x, w.y, t.q, t.q2);
+        M::ct(v[G0 + r * 2 * half + jj], v[G0 + r * 2 * half + jj + half], w.x, w.y, t);
     });
   });
 }
@@ -173,7 +280,7 @@ __device__ __forceinline__ void ct_group(u64 (&v)[NV], const ulonglong2* tw, u32
 // Inverse group: sub-stages KK-1 .. 0.  EXACT_TOP applies the exact rule to
 // sub-stage KK-1 (global stage m = n/2); FOLD folds n^-1 into sub-stage 0
 // (global stage m = 1, root index 1) and leaves canonical outputs.
-template <int KK, int G0, bool EXACT_TOP, bool FOLD, int NV>
+template <class M, int KK, int G0, bool EXACT_TOP, bool FOLD, int NV>
 __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32 base, const Tw& t) {
   static_for<0, KK>([&](auto uc) {
     constexpr int u = KK - 1 - decltype(uc)::value;
@@ -185,10 +292,9 @@ __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32
         u64& y = v[G0 + jj + half];
         u64 s, d;
         if constexpr (EXACT_TOP && u == KK - 1) {
-          gs_first_sd(x, y, t, s, d);
+          gs_first_sd<M>(x, y, t, s, d);
         } else {
-          s = x + y;
-          d = x - y + t.q2;
+          M::sd(x, y, t, s, d);
         }
         x = shoup(s, t.ninv, t.ninv_s, t.q);
         y = shoup(d, t.w1ninv, t.w1ninv_s, t.q);
@@ -203,11 +309,11 @@ __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32
           u64& y = v[G0 + r * 2 * half + jj + half];
           if constexpr (EXACT_TOP && u == KK - 1) {
             u64 s, d;
-            gs_first_sd(x, y, t, s, d);
+            gs_first_sd<M>(x, y, t, s, d);
             x = csub(s, t.q2);
             y = shoup_lazy(d, w.x, w.y, t.q);
           } else {
-            gs_bfly(x, y, w.x, w.y, t.q, t.q2);
+            M::gs(x, y, w.x, w.y, t);
           }
         }
       });
@@ -226,8 +332,9 @@ __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32
 // a direction share one loop body (the stage offset is a runtime value), and
 // the fused polymul runs its two forward transforms through the same code.
 
-template <int LOGN_, int E_, int U_ = 1>
+template <int LOGN_, int E_, int U_ = 1, class M_ = Mod62>
 struct Shape {
+  using M = M_;  // modulus class
   static constexpr int LOGN = LOGN_, E = E_;
   static constexpr int U = U_;  // radix-16 groups of a thread in flight at once (1 or 2)
   static constexpr int N = 1 << LOGN, T = N / E;
@@ -279,8 +386,8 @@ __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, c
       constexpr int i = decltype(ic)::value;
 #pragma unroll
       for (int jj = 0; jj < (1 << (KK - 1)); jj++)
-        ct_first(v[i * (1 << KK) + jj], v[i * (1 << KK) + jj + (1 << (KK - 1))], w0.x, w0.y, t);
-      ct_group<KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
+        ct_first<typename S::M>(v[i * (1 << KK) + jj], v[i * (1 << KK) + jj + (1 << (KK - 1))], w0.x, w0.y, t);
+      ct_group<typename S::M, KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
       const int g = (int)threadIdx.x + (i0 + i) * S::T;
 #pragma unroll
       for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
@@ -302,7 +409,8 @@ __device__ __forceinline__ void fwd_first_smem(u64* sm, const Tw& t, u32 tw_mult
     for (int i = 0; i < GR; i++)
 #pragma unroll
       for (int j = 0; j < (1 << KK); j++) v[i * (1 << KK) + j] = sm[pad(g0 + i * S::T + j * TMIN)];
-    static_for<0, GR>([&](auto ic) { ct_group<KK, 0, decltype(ic)::value * (1 << KK)>(v, t.fwd, tw_mult, t); });
+    static_for<0, GR>(
+        [&](auto ic) { ct_group<typename S::M, KK, 0, decltype(ic)::value * (1 << KK)>(v, t.fwd, tw_mult, t); });
 #pragma unroll
     for (int i = 0; i < GR; i++)
 #pragma unroll
@@ -327,7 +435,7 @@ __device__ __forceinline__ void fwd_passes(u64* sm, const Tw& t, u32 tw_mult, Ep
       u64 v[16];
 #pragma unroll
       for (int j = 0; j < 16; j++) v[j] = sm[pad(a0 + j * st)];
-      ct_group<4, 0, 0>(v, t.fwd, ps.base(g), t);
+      ct_group<typename S::M, 4, 0, 0>(v, t.fwd, ps.base(g), t);
       if (s0 < S::HEAD) {
 #pragma unroll
         for (int j = 0; j < 16; j++) sm[pad(a0 + j * st)] = v[j];
@@ -354,7 +462,7 @@ __device__ __forceinline__ void inv_passes(u64* sm, const Tw& t, u32 tw_mult, in
       u64 v[16];
 #pragma unroll
       for (int j = 0; j < 16; j++) v[j] = sm[pad(a0 + j * st)];
-      gs_group<4, 0, false, false>(v, t.inv, ps.base(g), t);
+      gs_group<typename S::M, 4, 0, false, false>(v, t.inv, ps.base(g), t);
 #pragma unroll
       for (int j = 0; j < 16; j++) sm[pad(a0 + j * st)] = v[j];
     }
@@ -376,7 +484,7 @@ __device__ __forceinline__ void inv_last_smem(u64* sm, const Tw& t, u32 tw_mult)
 #pragma unroll
       for (int j = 0; j < (1 << KK); j++) v[i * (1 << KK) + j] = sm[pad(g0 + i * S::T + j * TMIN)];
     static_for<0, GR>(
-        [&](auto ic) { gs_group<KK, decltype(ic)::value * (1 << KK), false, false>(v, t.inv, tw_mult, t); });
+        [&](auto ic) { gs_group<typename S::M, KK, decltype(ic)::value * (1 << KK), false, false>(v, t.inv, tw_mult, t); });
 #pragma unroll
     for (int i = 0; i < GR; i++)
 #pragma unroll
@@ -437,9 +545,9 @@ __device__ __forceinline__ void inv_last_epi(u64* sm, const Tw& t, u32 tw_mult, 
 #pragma unroll
     for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];
     if (fold)
-      gs_group<KK, 0, false, true>(v, t.inv, tw_mult, t);
+      gs_group<typename S::M, KK, 0, false, true>(v, t.inv, tw_mult, t);
     else
-      gs_group<KK, 0, false, false>(v, t.inv, tw_mult, t);
+      gs_group<typename S::M, KK, 0, false, false>(v, t.inv, tw_mult, t);
 #pragma unroll
     for (int j = 0; j < (1 << KK); j++) out[g + j * TMIN] = epi(v[j]);
   }
@@ -493,10 +601,10 @@ __device__ __forceinline__ J fetch_job(const J* jobs, const J& one, int jid) {
 // (transforms of 2^(LOGN + sub_log) words after / before the global passes),
 // sub-block `sub` using twiddle multiplier 2^sub_log + sub.
 
-template <int LOGN, int E, int U>
+template <int LOGN, int E, int U, class M = Mod62>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     k_ntt_fwd(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log) {
-  using S = Shape<LOGN, E, U>;
+  using S = Shape<LOGN, E, U, M>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
 #pragma unroll 1
@@ -510,18 +618,18 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     fwd_first<S>(sm, in, t, tw_mult);
     fwd_passes<S>(sm, t, tw_mult, [&](int g, u64(&v)[16]) {
 #pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+      for (int j = 0; j < 16; j++) v[j] = M::canon(v[j], t);
       store16(v, out + 16 * g);
     });
   }
 }
 
 // LIFT: the epilogue `lift` follows the last stage (sub_log == 0 only).
-template <int LOGN, int E, int U, bool LIFT = false>
+template <int LOGN, int E, int U, bool LIFT = false, class M = Mod62>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
     k_ntt_inv(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int sub_log,
               const __grid_constant__ vkcu_lift lift) {
-  using S = Shape<LOGN, E, U>;
+  using S = Shape<LOGN, E, U, M>;
   extern __shared__ u64 sm[];
   const int total = njobs << sub_log;
 #pragma unroll 1
@@ -548,7 +656,7 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
       const int g = (int)threadIdx.x + i * S::T;
       u64 v[16];
       load16(v, in + 16 * g);
-      gs_group<4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
+      gs_group<M, 4, 0, true, false>(v, t.inv, tw_mult * (u32)(S::N / 16) + (u32)g, t);
 #pragma unroll
       for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
     }
@@ -565,11 +673,11 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E>())
 // and runs the first inverse pass on the products in the same registers; the
 // rest of the inverse transform then writes c.  a is prefetched
 // into L2 while b is transformed, the next job's b while a is.
-template <int LOGN, int E, int U, bool LIFT = false>
+template <int LOGN, int E, int U, bool LIFT = false, class M = Mod62>
 __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E, true>())
     k_polymul(const vkcu_poly_job* __restrict__ jobs, int njobs, vkcu_poly_job one,
               const __grid_constant__ vkcu_lift lift) {
-  using S = Shape<LOGN, E, U>;
+  using S = Shape<LOGN, E, U, M>;
   extern __shared__ u64 sm[];
   constexpr unsigned kChunk = (unsigned)(S::N * 8 / 4);
 #pragma unroll 1
@@ -588,15 +696,15 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E, true>())
       fwd_passes<S>(sm, t, 1u, [&](int g, u64(&v)[16]) {
         if (ph == 0) {
 #pragma unroll
-          for (int j = 0; j < 16; j++) v[j] = canon4(v[j], t.q, t.q2);
+          for (int j = 0; j < 16; j++) v[j] = M::canon(v[j], t);
           store16(v, scratch + 16 * g);
         } else {
           u64 bh[16];
           load16(bh, scratch + 16 * g);
 #pragma unroll
-          for (int j = 0; j < 16; j++) v[j] = barrett_mul_lazy(canon4(v[j], t.q, t.q2), bh[j], t.q, t.q2, t.mu, t.qbits);
+          for (int j = 0; j < 16; j++) v[j] = M::product(v[j], bh[j], t);
           // the first inverse pass (stages HEAD + 3 .. HEAD) on the same 16 words
-          gs_group<4, 0, false, false>(v, t.inv, (1u << S::HEAD) + (u32)g, t);
+          gs_group<M, 4, 0, M::EXACT_AFTER_PRODUCT, false>(v, t.inv, (1u << S::HEAD) + (u32)g, t);
 #pragma unroll
           for (int j = 0; j < 16; j++) sm[pad(16 * g + j)] = v[j];
         }
@@ -632,6 +740,21 @@ int inv_cluster(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu
                 const vkcu_lift* lift = nullptr);
 int poly_cluster(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc, int logs,
                  const vkcu_lift* lift = nullptr);
+
+// The same families for 2^62 <= q < 2^63 (Mod63), default shape of each
+// degree, sub-blocks of 2^14 words for the cluster kernels (translation units
+// ntt_wide_*.cu).
+int fwd_cta_wide(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n,
+                 int sub_log, int sms);
+int inv_cta_wide(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int log_n,
+                 int sub_log, int sms, const vkcu_lift* lift);
+int poly_cta_wide(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int log_n, int sms,
+                  const vkcu_lift* lift);
+int fwd_cluster_wide(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc);
+int inv_cluster_wide(cudaStream_t st, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job& one, int logc,
+                     const vkcu_lift* lift);
+int poly_cluster_wide(cudaStream_t st, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job& one, int logc,
+                      const vkcu_lift* lift);
 
 // Launch set-up of one kernel, per device: the dynamic shared-memory opt-in
 // and the occupancy figure its grid is sized from (resident blocks per SM,
@@ -676,6 +799,19 @@ static int setup_cta(K kernel, int threads, int smem, KernelSetup& ks, int* per_
 __host__ inline int grid_from(int per_sm, long work, int sms) {
   const long cap = (long)per_sm * (sms > 0 ? sms : 1);
   return (int)(work < cap ? work : cap);
+}
+
+// One launch of the CTA-resident kernel `kern` of shape S over `work` work
+// items (one-time set-up per kernel and device; grid = one wave of resident
+// blocks, or fewer when there is less work).
+template <class S, auto kern, class... Args>
+static int launch_cta(cudaStream_t st, long work, int sms, Args... args) {
+  static KernelSetup setup;
+  int per_sm = 1;
+  if (const int e = setup_cta(kern, S::T, S::SMEM_BYTES, setup, &per_sm)) return e;
+  kern<<<grid_from(per_sm, work, sms), S::T, S::SMEM_BYTES, st>>>(args...);
+  vkcu_count_launches(1);
+  return (int)cudaGetLastError();
 }
 
 // Shapes per degree and variant: words per thread E and group unroll U.

@@ -35,7 +35,10 @@
 
 #include "internal.h"
 
-#define SRV_MAX_CLASSES 32
+/* classes of one micro-batch: one per (degree, modulus class) present; the
+ * first SRV_AUX + 1 of them can run on concurrent streams */
+#define SRV_MAX_CLASSES 64
+#define SRV_AUX 32
 /* At low load (the micro-batch took every queued request) a micro-batch of
  * at most SRV_CHUNKS requests and at least 2 SRV_CHUNK_MIN bytes of operands
  * is issued in up to SRV_CHUNKS chunks of limbs: chunk c computes (on its
@@ -86,7 +89,7 @@ struct vkhel_server {
 	void *s_chunk[SRV_CHUNKS - 1]; /* compute streams of chunks 1 .. SRV_CHUNKS-1 (chunk 0: s_comp) */
 	/* concurrent degree classes of a micro-batch (tuning flag) */
 	int forked;
-	void *aux[SRV_MAX_CLASSES], *join[SRV_MAX_CLASSES], *fork;
+	void *aux[SRV_AUX], *join[SRV_AUX], *fork;
 	uint64_t budget, bytes;
 	uint32_t max_limbs, nslots;
 	struct srv_slot *slots;
@@ -172,11 +175,13 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 	qsort(keys + j0, j1 - j0, sizeof(uint64_t), cmp_job_log_n);
 	for (uint32_t i = j0; i < j1; i++) {
 		const uint32_t log_n = (uint32_t) (keys[i] >> 40);
-		sl->host_poly[i] = tmp[keys[i] & 0xffffffffffull];
-		if (nclasses == 0 || classes[nclasses - 1].log_n != log_n) {
+		const int wide = (int) ((keys[i] >> 39) & 1);
+		sl->host_poly[i] = tmp[keys[i] & 0x7fffffffffull];
+		if (nclasses == 0 || classes[nclasses - 1].log_n != log_n || classes[nclasses - 1].wide != wide) {
 			struct vkh_job_class *cl = &classes[nclasses++];
 			cl->kind = VKH_JOB_POLYMUL;
 			cl->log_n = log_n;
+			cl->wide = wide;
 			cl->lift = 0;
 			cl->first = i;
 			cl->count = 0;
@@ -197,7 +202,7 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 	if (!e)
 		e = vkcu_stream_wait(cs, sl->ev_in[c]);
 	if (!e) /* a whole micro-batch: its classes on concurrent streams when tuned so */
-		e = s->forked && nchunks == 1
+		e = s->forked && nchunks == 1 && nclasses <= SRV_AUX + 1
 				? vkh_issue_classes_forked(cs, s->aux, s->fork, s->join, ctx->sms, dpoly, dntt, classes, nclasses, NULL)
 				: vkh_issue_classes(cs, ctx->sms, dpoly, dntt, classes, nclasses, NULL);
 	if (!e)
@@ -221,7 +226,8 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 	struct vkhel_ctx *ctx = s->ctx;
 	vkcu_range_push("vkhel_server micro-batch");
 	const uint64_t cap = ((uint64_t) s->max_limbs + 64) * 2;
-	/* keys: log_n in the high bits, running index in the low bits -> stable sort */
+	/* keys: log_n in the high bits, then the modulus class, running index in
+	 * the low bits -> stable sort into classes of one degree and class */
 	uint64_t *keys = malloc(sizeof(uint64_t) * cap);
 	vkcu_poly_job *tmp = malloc(sizeof(vkcu_poly_job) * cap);
 	struct srv_seg *segs = malloc(sizeof(struct srv_seg) * (sl->nreqs + SRV_CHUNKS));
@@ -249,7 +255,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 			j.c = base + 2 * words + (uint64_t) k * r->n;
 			j.scratch = fused ? j.c : base + 3 * words + (uint64_t) k * r->n;
 			j.tw = d->dev_set;
-			keys[njobs] = ((uint64_t) r->log_n << 40) | njobs;
+			keys[njobs] = ((uint64_t) r->log_n << 40) | ((uint64_t) vkcu_wide(r->tables[k]->q) << 39) | njobs;
 			tmp[njobs++] = j;
 			acc += 16 * r->n;
 			const int last = i + 1 == sl->nreqs && k + 1 == r->limbs;
@@ -452,7 +458,7 @@ struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg) 
 	s->forked = vkh_variant(3, 0) == 1;
 	if (!e && s->forked)
 		e = vkcu_event_create(&s->fork);
-	for (uint32_t k = 0; !e && s->forked && k < SRV_MAX_CLASSES; k++) {
+	for (uint32_t k = 0; !e && s->forked && k < SRV_AUX; k++) {
 		e = vkcu_stream_create(&s->aux[k]);
 		if (!e)
 			e = vkcu_event_create(&s->join[k]);
@@ -509,7 +515,7 @@ int64_t vkhel_server_submit(struct vkhel_server *s, struct vkhel_ntt_tables *con
 		const struct vkhel_ntt_tables *t = tables[k];
 		if (!t || t->n != n || n < 2)
 			return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit: limb %u tables invalid", k);
-		if (t->q >= ((uint64_t) 1 << 62) || t->q < 3 || t->log_n > vkcu_max_log_n())
+		if (t->q >= ((uint64_t) 1 << 63) || t->q < 3 || t->unreduced || t->log_n > vkcu_max_log_n())
 			return -vkh_fail(NULL, VKHEL_ERR_UNSUPPORTED, "server_submit: limb %u (n, q) unsupported", k);
 	}
 	struct srv_req *r = calloc(1, sizeof(*r));
@@ -715,7 +721,7 @@ void vkhel_server_destroy(struct vkhel_server *s) {
 	for (int i = 0; i < 3; i++)
 		if (streams[i])
 			vkcu_stream_destroy(streams[i]);
-	for (int k = 0; k < SRV_MAX_CLASSES; k++) {
+	for (int k = 0; k < SRV_AUX; k++) {
 		if (s->aux[k]) {
 			vkcu_sync(s->aux[k]);
 			vkcu_stream_destroy(s->aux[k]);

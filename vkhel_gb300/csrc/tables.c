@@ -51,7 +51,10 @@ static void compute_host_arrays(struct vkhel_ntt_tables *t) {
 		t->roots[bit_reverse(i, t->log_n)] = power;
 		canonical &= power < q && power != 0;
 	}
-	const int negacyclic = canonical && n > 1 && vkh_mulmod(power, w, q) == q - 1;
+	/* The index rule needs true powers of w: canonical Barrett products are
+	 * (their estimate never overflows below 2^62); at 63 bits the reference's
+	 * product can wrap, so there every entry is inverted as it does. */
+	const int negacyclic = canonical && t->qbits <= 62 && n > 1 && vkh_mulmod(power, w, q) == q - 1;
 	t->inv_roots[0] = vkh_invmod(1, q);
 	for (uint64_t i = 1; i < n; i++) {
 		const uint64_t slot = bit_reverse(i, t->log_n);
@@ -63,6 +66,7 @@ static void compute_host_arrays(struct vkhel_ntt_tables *t) {
 	for (uint64_t i = 0; i < n; i++) {
 		t->roots_shoup[i] = vkh_shoup(t->roots[i], q);
 		t->inv_roots_shoup[i] = vkh_shoup(t->inv_roots[i], q);
+		t->unreduced |= t->roots[i] >= q || t->inv_roots[i] >= q;
 	}
 }
 

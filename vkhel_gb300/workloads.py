@@ -92,3 +92,46 @@ def ragged_instances(count=512, seed=3, log_n_range=(12, 16), max_limbs=16):
     log_ns = rng.integers(log_n_range[0], log_n_range[1] + 1, size=count)
     limbs = rng.integers(1, max_limbs + 1, size=count)
     return [(int(l), int(k)) for l, k in zip(log_ns, limbs)]
+
+
+def ragged_batch(count=512, seed=3, log_n_range=(12, 16), max_limbs=16):
+    """The ragged batch's operands: a list of (n, qs, ws, a, b), one per
+    instance of ragged_instances(count, seed), with the instance's limbs
+    taking the first `limbs` primes of its degree and a, b limb-major
+    (limbs * n words); the operands come from default_rng(seed) drawn in
+    instance order, all of a's limbs before b's."""
+    rng = np.random.default_rng(seed)
+    primes = {}
+    out = []
+    for log_n, limbs in ragged_instances(count, seed, log_n_range, max_limbs):
+        n = 1 << log_n
+        if n not in primes:
+            qq = ntt_primes(n, max_limbs)
+            primes[n] = (qq, [root_for(n, q) for q in qq])
+        qs, ws = primes[n][0][:limbs], primes[n][1][:limbs]
+        a = np.concatenate([uniform(rng, q, n) for q in qs])
+        b = np.concatenate([uniform(rng, q, n) for q in qs])
+        out.append((n, qs, ws, a, b))
+    return out
+
+
+def serving_requests(count, seed=4, log_n_range=(12, 17), max_limbs=24):
+    """Polymul requests of the serving sweep: n = 2^k with k uniform in
+    log_n_range, limbs uniform in 1..max_limbs (the first `limbs` primes of
+    the degree), operands uniform mod each limb's prime, all from
+    default_rng(seed): per request its shape, then a's limbs, then b's.
+    Returns a list of (n, qs, ws, a, b), a and b limb-major."""
+    rng = np.random.default_rng(seed)
+    primes = {}
+    out = []
+    for _ in range(count):
+        n = 1 << int(rng.integers(log_n_range[0], log_n_range[1] + 1))
+        limbs = int(rng.integers(1, max_limbs + 1))
+        if n not in primes:
+            qq = ntt_primes(n, max_limbs)
+            primes[n] = (qq, [root_for(n, q) for q in qq])
+        qs, ws = primes[n][0][:limbs], primes[n][1][:limbs]
+        a = np.concatenate([uniform(rng, q, n) for q in qs])
+        b = np.concatenate([uniform(rng, q, n) for q in qs])
+        out.append((n, qs, ws, a, b))
+    return out
