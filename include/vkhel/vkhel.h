@@ -23,8 +23,11 @@
  * Differences: failures that the reference turns into assert() aborts are
  * reported instead (NULL from constructors, a recorded error that
  * vkhel_ctx_last_error() returns); set VKHEL_STRICT=1 to abort like the
- * reference.  Unsupported transform parameters (n not a power of two,
- * q >= 2^62) are rejected rather than computed with undefined behaviour.
+ * reference.  Unsupported transform parameters are rejected rather than
+ * computed with undefined behaviour: n not a power of two or above 2^26,
+ * q >= 2^63 (where the reference's inverse-mod and butterfly sums overflow,
+ * src/numbers.c:71-99), and the rare 63-bit (n, q, w) whose table the
+ * reference's builder leaves with an entry not below q.
  */
 #ifndef VKHEL_H
 #define VKHEL_H

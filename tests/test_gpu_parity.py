@@ -220,7 +220,7 @@ def test_transform_rejects_unsupported(vk, ctx):
     with pytest.raises(vk.VkhelError) as e:
         vk.forward_transform(a, a, t)
     assert e.value.code == 8 and "not below q" in e.value.msg
-    t = vk.NttTables(32, 2251799813685313, 3)
+    t = vk.NttTables(128, 2251799813685313, 3)
     with pytest.raises(vk.VkhelError):
         vk.forward_transform(a, a, t)  # vector shorter than n
 

@@ -171,13 +171,22 @@ def test_tuning_table_parsing_and_overrides(vk, tmp_path):
         if lib_clear_error:
             lib_clear_error(None)
         entries = set()
+        buckets = set()
         for line in open(table):
             line = line.split("#")[0].split()
-            if len(line) == 3:
+            if len(line) in (3, 4):
                 entries.add((int(line[0]), int(line[1])))
+                if len(line) == 4:
+                    buckets.add((int(line[0]), int(line[1]), int(line[3])))
         for fam in (0, 1, 2):
             assert {(fam, n) for n in range(8, 15)} <= entries, f"family {fam} incomplete"
+            assert {(fam, n, b) for n in range(8, 15) for b in range(4)} <= buckets, f"family {fam} buckets"
         assert (3, 0) in entries
+        # a bucket field sets that job-count bucket only; vkhel_tune_get reads the many-jobs bucket (3)
+        t.write_text("0 13 2\n0 13 1 0\n")
+        assert L.vkhel_tune_load(str(t).encode()) == 0 and L.vkhel_tune_get(0, 13) == 2
+        t.write_text("0 13 1 3\n0 13 0 9\n")
+        assert L.vkhel_tune_load(str(t).encode()) == 0 and L.vkhel_tune_get(0, 13) == 1
     finally:
         for (f, n), v in saved.items():
             L.vkhel_tune_set(f, n, v)

@@ -1,0 +1,157 @@
+"""Small workloads, one per kernel family, for profiling a kernel alone.
+
+    python -m vkhel_gb300.cases NAME [--reps R]
+    python -m vkhel_gb300.cases all
+
+Each case builds its inputs (seeded, uniform mod 60-bit primes unless the
+name says otherwise), runs its launch once as a warm-up and then R more
+times (default 2), synchronizes and prints one line.  The inputs exceed the
+129 MB L2 where the kernel streams from HBM, and stay at a few hundred MB on
+the device so that a profiler capture of one launch ends quickly.
+
+  fwd_batch     1024 forward transforms of n = 2^14 (batch)     k_ntt_fwd<14,..>
+  inv_batch     1024 inverse transforms of n = 2^14 (batch)     k_ntt_inv<14,..>
+  fwd_cluster   64 forward transforms of n = 2^16 (batch)       k_ntt_fwd_cluster<2,..>
+  inv_cluster   64 inverse transforms of n = 2^16 (batch)       k_ntt_inv_cluster<2,..>
+  twiddles      device twiddle tables for n = 2^20              k_twiddles
+  global        16 forward + 16 inverse transforms of n = 2^20  k_fwd_global, k_inv_global
+  pointwise     32 polymuls of n = 2^18 (composed path)         k_pointwise
+  simple        4096 forward + inverse transforms of n = 2^7    k_ntt_fwd_simple, k_ntt_inv_simple
+  wide_polymul  256 polymuls of n = 2^14, 63-bit primes         k_polymul<14,..,Mod63>
+  elementwise   elemgtsub / elemmod / elemgtadd / elemfma on 2^25 words   k_elementwise<...>
+"""
+import argparse
+import sys
+
+import numpy as np
+
+import vkhel_gb300 as vk
+from vkhel_gb300 import workloads
+
+
+def _tabs(n, count, bits=60):
+    qs = workloads.ntt_primes(n, count, bound=1 << bits)
+    return qs, [vk.NttTables(n, q, workloads.root_for(n, q)) for q in qs]
+
+
+def _operands(ctx, n, qs, jobs, seed):
+    rng = np.random.default_rng(seed)
+    h = np.concatenate([workloads.uniform(rng, qs[j % len(qs)], n) for j in range(jobs)])
+    return vk.Vector(ctx, h)
+
+
+def _transform_batch(ctx, n, jobs, inverse, primes=8):
+    qs, tabs = _tabs(n, primes)
+    x = _operands(ctx, n, qs, jobs, n + jobs)
+    y = vk.Vector(ctx, jobs * n)
+    bt = vk.Batch(ctx)
+    bt.add_transform([tabs[j % primes] for j in range(jobs)], x, y, inverse=inverse)
+    bt.commit(graph=True)
+    return bt.launch, (bt, x, y, tabs)
+
+
+def _polymul_batch(ctx, n, jobs, bits=60, primes=8):
+    qs, tabs = _tabs(n, primes, bits)
+    a, b = _operands(ctx, n, qs, jobs, 1), _operands(ctx, n, qs, jobs, 2)
+    c = vk.Vector(ctx, jobs * n)
+    bt = vk.Batch(ctx)
+    for j in range(0, jobs, primes):
+        k = min(primes, jobs - j)
+        bt.add_polymul(tabs[:k], a.device_ptr + 8 * j * n, b.device_ptr + 8 * j * n, c.device_ptr + 8 * j * n)
+    bt.commit(graph=True)
+    return bt.launch, (bt, a, b, c, tabs)
+
+
+def case_fwd_batch(ctx):
+    return _transform_batch(ctx, 1 << 14, 1024, False)
+
+
+def case_inv_batch(ctx):
+    return _transform_batch(ctx, 1 << 14, 1024, True)
+
+
+def case_fwd_cluster(ctx):
+    return _transform_batch(ctx, 1 << 16, 64, False)
+
+
+def case_inv_cluster(ctx):
+    return _transform_batch(ctx, 1 << 16, 64, True)
+
+
+def case_twiddles(ctx):
+    n = 1 << 20
+    q = workloads.ntt_primes(n, 1)[0]
+    w = workloads.root_for(n, q)
+    keep = []
+
+    def run():  # another primitive 2n-th root w^(2k+1) per call: fresh tables, generated on the device
+        t = vk.NttTables(n, q, pow(w, 2 * len(keep) + 1, q))
+        t.device_arrays(ctx)
+        keep.append(t)
+    return run, keep
+
+
+def case_global(ctx):
+    n, jobs = 1 << 20, 16
+    fwd, kf = _transform_batch(ctx, n, jobs, False, primes=4)
+    inv, ki = _transform_batch(ctx, n, jobs, True, primes=4)
+    return (lambda: (fwd(), inv())), (kf, ki)
+
+
+def case_pointwise(ctx):
+    return _polymul_batch(ctx, 1 << 18, 32, primes=4)
+
+
+def case_simple(ctx):
+    n, jobs = 1 << 7, 4096
+    fwd, kf = _transform_batch(ctx, n, jobs, False)
+    inv, ki = _transform_batch(ctx, n, jobs, True)
+    return (lambda: (fwd(), inv())), (kf, ki)
+
+
+def case_wide_polymul(ctx):
+    return _polymul_batch(ctx, 1 << 14, 256, bits=63)
+
+
+def case_elementwise(ctx):
+    words = 1 << 25
+    q = (1 << 61) - 1
+    rng = np.random.default_rng(7)
+    a = vk.Vector(ctx, workloads.uniform(rng, q, words))
+    b = vk.Vector(ctx, workloads.uniform(rng, q, words))
+    r = vk.Vector(ctx, words)
+
+    def run():
+        vk.elemgtsub(a, r, q // 2, q, 65537)
+        vk.elemmod(a, r, 65537, q)
+        vk.elemgtadd(a, r, q // 2, 17)
+        vk.elemfma(a, b, r, 12345, q)
+    return run, (a, b, r)
+
+
+CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
+
+
+def run_case(name, reps=2):
+    with vk.Context() as ctx:
+        fn, keep = CASES[name](ctx)
+        fn()  # warm-up: one-time set-up and first graph launch
+        ctx.sync()
+        for _ in range(reps):
+            fn()
+        ctx.sync()
+        del keep
+    print(f"case {name}: {reps} launches after one warm-up", flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("name", choices=sorted(CASES) + ["all"])
+    ap.add_argument("--reps", type=int, default=2)
+    args = ap.parse_args(argv)
+    for name in sorted(CASES) if args.name == "all" else [args.name]:
+        run_case(name, args.reps)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

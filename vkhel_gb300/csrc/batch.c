@@ -48,6 +48,13 @@ struct vkhel_batch {
 	vkcu_ntt_job *dev_ntt; /* [3 * njobs]: b->scratch, a->c, c->c */
 	void *graph;
 	uint32_t kernels;
+	/* a ragged batch as one launch (tuning family 3, log_n 2): item table,
+	 * job copies (plus a dummy copy for an odd pair), two counters and the
+	 * dummy products' output, in one device allocation */
+	int ragged;
+	uint32_t n_cluster_items, n_items;
+	void *ragged_dev;
+	uint64_t ragged_bytes;
 	/* concurrent degree classes: one stream and one join event per class
 	 * after the first, one fork event */
 	uint32_t naux;
@@ -314,11 +321,97 @@ int vkh_issue_classes_forked(void *stream, void *const *aux, void *fork, void *c
 }
 
 static int issue(struct vkhel_batch *b) {
+	if (b->ragged) {
+		const char *base = b->ragged_dev;
+		const uint64_t items_bytes = (sizeof(vkcu_ragged_item) * b->n_items + 255) & ~(uint64_t) 255;
+		const uint64_t jobs_bytes = (sizeof(vkcu_poly_job) * (b->njobs + 2) + 255) & ~(uint64_t) 255;
+		return vkcu_polymul_ragged(b->ctx->stream, (const vkcu_ragged_item *) base, (int) b->n_cluster_items,
+				(int) b->n_items, (const vkcu_poly_job *) (base + items_bytes),
+				(unsigned *) (base + items_bytes + jobs_bytes), b->ctx->sms);
+	}
 	if (b->naux)
 		return vkh_issue_classes_forked(b->ctx->stream, b->aux, b->fork, b->join, b->ctx->sms, b->dev_poly,
 				b->dev_ntt, b->classes, b->nclasses, b->lifts);
 	return vkh_issue_classes(b->ctx->stream, b->ctx->sms, b->dev_poly, b->dev_ntt, b->classes, b->nclasses,
 			b->lifts);
+}
+
+/* The single-launch form of a ragged batch (ntt_ragged.cu) when the tuning
+ * table asks for it and every class is a fused product of degree 2^12 ..
+ * 2^16 with q < 2^62 and no epilogue: items in decreasing size, 2^15 and
+ * 2^12 products in pairs, an odd pair completed by a copy of its product
+ * that writes a dummy buffer. */
+static int ragged_setup(struct vkhel_batch *b) {
+	b->ragged = 0;
+	if (b->nclasses < 2 || vkh_variant(3, 2) != 1)
+		return VKHEL_OK;
+	uint32_t first[17] = {0}, count[17] = {0};
+	for (uint32_t k = 0; k < b->nclasses; k++) {
+		const struct vkh_job_class *cl = &b->classes[k];
+		if (cl->kind != VKH_JOB_POLYMUL || !cl->fused || cl->wide || cl->lift || cl->log_n < 12 || cl->log_n > 16 ||
+				count[cl->log_n])
+			return VKHEL_OK;
+		first[cl->log_n] = cl->first;
+		count[cl->log_n] = cl->count;
+	}
+	const uint32_t dummy15 = b->njobs, dummy12 = b->njobs + 1; /* job indices of the dummy copies */
+	const uint32_t n_cluster = count[16] + (count[15] + 1) / 2;
+	const uint32_t n_items = n_cluster + count[14] + count[13] + (count[12] + 1) / 2;
+	const uint64_t items_bytes = (sizeof(vkcu_ragged_item) * n_items + 255) & ~(uint64_t) 255;
+	const uint64_t jobs_bytes = (sizeof(vkcu_poly_job) * (b->njobs + 2) + 255) & ~(uint64_t) 255;
+	const uint64_t dummy_off = items_bytes + jobs_bytes + 256;
+	const uint64_t bytes = dummy_off + sizeof(uint64_t) * (((uint64_t) 1 << 15) + ((uint64_t) 1 << 12));
+	char *host = calloc(1, dummy_off);
+	if (!host)
+		return vkh_fail(b->ctx, VKHEL_ERR_OUT_OF_MEMORY, "batch_commit: host allocation failed");
+	int st = vkh_dev_alloc(b->ctx, bytes, &b->ragged_dev);
+	if (st) {
+		free(host);
+		return st;
+	}
+	b->ragged_bytes = bytes;
+	vkcu_ragged_item *items = (vkcu_ragged_item *) host;
+	vkcu_poly_job *jobs = (vkcu_poly_job *) (host + items_bytes);
+	uint64_t *dummy = (uint64_t *) ((char *) b->ragged_dev + dummy_off);
+	for (uint32_t i = 0; i < b->njobs; i++)
+		jobs[i] = b->recs[i].job;
+	uint32_t m = 0;
+	for (uint32_t i = 0; i < count[16]; i++)
+		items[m++] = (vkcu_ragged_item){16, first[16] + i, 0};
+	for (uint32_t i = 0; i < count[15]; i += 2) {
+		const uint32_t j = first[15] + i;
+		uint32_t j1 = j + 1;
+		if (i + 1 == count[15]) { /* odd: the second pair runs a copy into the dummy buffer */
+			jobs[dummy15] = jobs[j];
+			jobs[dummy15].c = jobs[dummy15].scratch = dummy;
+			j1 = dummy15;
+		}
+		items[m++] = (vkcu_ragged_item){15, j, j1};
+	}
+	for (uint32_t i = 0; i < count[14]; i++)
+		items[m++] = (vkcu_ragged_item){14, first[14] + i, 0};
+	for (uint32_t i = 0; i < count[13]; i++)
+		items[m++] = (vkcu_ragged_item){13, first[13] + i, 0};
+	for (uint32_t i = 0; i < count[12]; i += 2) {
+		const uint32_t j = first[12] + i;
+		uint32_t j1 = j + 1;
+		if (i + 1 == count[12]) {
+			jobs[dummy12] = jobs[j];
+			jobs[dummy12].c = jobs[dummy12].scratch = dummy + ((uint64_t) 1 << 15);
+			j1 = dummy12;
+		}
+		items[m++] = (vkcu_ragged_item){12, j, j1};
+	}
+	int e = vkcu_h2d(b->ctx->stream, b->ragged_dev, host, items_bytes + jobs_bytes);
+	if (!e)
+		e = vkcu_sync(b->ctx->stream);
+	free(host);
+	if (e)
+		return vkh_cuda(b->ctx, e, "batch_commit: ragged item table upload");
+	b->n_cluster_items = n_cluster;
+	b->n_items = n_items;
+	b->ragged = 1;
+	return VKHEL_OK;
 }
 
 int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
@@ -396,7 +489,9 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	b->dev_poly = b->dev;
 	b->dev_ntt = (vkcu_ntt_job *) ((char *) b->dev + ntt_off);
 
-	if (b->nclasses > 1 && vkh_variant(3, 0) == 1) {
+	if ((st = ragged_setup(b)))
+		return st;
+	if (!b->ragged && b->nclasses > 1 && vkh_variant(3, 0) == 1) {
 		e = vkcu_event_create(&b->fork);
 		for (uint32_t k = 0; !e && k + 1 < b->nclasses; k++) {
 			e = vkcu_stream_create(&b->aux[k]);
@@ -474,6 +569,7 @@ void vkhel_batch_destroy(struct vkhel_batch *b) {
 	vkcu_event_destroy(b->fork);
 	vkh_dev_free(ctx, b->dev, b->dev_bytes);
 	vkh_dev_free(ctx, b->scratch, b->scratch_bytes);
+	vkh_dev_free(ctx, b->ragged_dev, b->ragged_bytes);
 	free(b->recs);
 	free(b->lifts);
 	free(b);

@@ -118,6 +118,7 @@ void vkh_fill_ntt_jobs(const vkcu_poly_job *poly, vkcu_ntt_job *ntt, const struc
 		uint32_t nclasses);
 /* tuning.c -- variant of kernel family (VKHEL_TUNE_*) for degree 2^log_n */
 int vkh_variant(int family, int log_n);
+int vkh_variant_jobs(int family, int log_n, long njobs, int sms);
 /* Lookup only: NULL when (n, q, w) has no device copy in ctx yet. */
 const struct vkh_devtab *vkh_devtab_find(const struct vkhel_ctx *ctx, const struct vkhel_ntt_tables *t);
 

@@ -176,9 +176,26 @@ int vkcu_lift_jobs(void *stream, const vkcu_ntt_job *jobs, int njobs, const vkcu
  * polymul that is not fused. */
 int vkcu_pointwise(void *stream, const vkcu_poly_job *jobs, int njobs,
 		uint32_t log_n, int wide, int sms);
+/* A ragged batch of fused limb products of degrees 2^12 .. 2^16 as one
+ * persistent launch (ntt_ragged.cu): items in decreasing size, the first
+ * n_cluster_items of kind 16 (one product of 2^16 on a cluster of four CTAs)
+ * or 15 (two products of 2^15, one per CTA pair), then kinds 14 and 13 (one
+ * product per CTA) and 12 (two products per CTA); job0 / job1 index `jobs`.
+ * `counters` is two words of device memory the launch resets first. */
+typedef struct vkcu_ragged_item {
+	uint32_t kind;
+	uint32_t job0, job1;
+} vkcu_ragged_item;
+int vkcu_polymul_ragged(void *stream, const vkcu_ragged_item *items, int n_cluster_items,
+		int n_items, const vkcu_poly_job *jobs, unsigned *counters, int sms);
+
 /* Kernel variant table (tuning.c): family 0 = fused polymul, 1 = forward,
- * 2 = inverse, 3 = batch options. */
+ * 2 = inverse, 3 = batch options (log_n 0: concurrent degree classes, 1:
+ * no split of single jobs over 8 CTAs, 2: ragged batches as one launch);
+ * per degree and, for a launch of njobs jobs
+ * on sms SMs, per job-count bucket (vkh_variant: the many-jobs entry). */
 int vkh_variant(int family, int log_n);
+int vkh_variant_jobs(int family, int log_n, long njobs, int sms);
 /* Integer-pipe microbenchmarks (peak.cu). */
 int vkcu_measure_int_peak(void *stream, int sms, double *bfly_per_s, double *imad_per_s);
 /* Largest log_n of the single-launch kernels (one CTA up to 2^14, one

@@ -255,7 +255,7 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
     if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta);
   } else {
     if (split_small(njobs, log_n, sms)) return fwd_cluster(st, jobs, njobs, o, 3, (int)log_n - 3);
-    if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(1, (int)log_n));
+    if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant_jobs(1, (int)log_n, njobs, sms));
     if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta);
   }
   const int np = global_passes((int)log_n);
@@ -268,7 +268,7 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
   }
   const int sub_log = (int)log_n - kMaxCta;
   return wide ? fwd_cta_wide(st, jobs, njobs, o, kMaxCta, sub_log, sms)
-              : fwd_cta(st, jobs, njobs, o, kMaxCta, sub_log, sms, vkh_variant(1, kMaxCta));
+              : fwd_cta(st, jobs, njobs, o, kMaxCta, sub_log, sms, vkh_variant_jobs(1, kMaxCta, (long)njobs << sub_log, sms));
 }
 
 static bool has_lift(const vkcu_lift* lift) { return lift && lift->count > 0; }
@@ -296,13 +296,13 @@ extern "C" int vkcu_ntt_inverse_lift(void* stream, const vkcu_ntt_job* jobs, int
     return inv_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
   } else if (!wide && log_n <= (uint32_t)kMaxCta) {
     if (lifted) return inv_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
-    return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant(2, (int)log_n));
+    return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant_jobs(2, (int)log_n, njobs, sms));
   } else if (!wide && log_n <= (uint32_t)kMaxCluster) {
     return inv_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lp);
   } else {
     const int sub_log = (int)log_n - kMaxCta;
     e = wide ? inv_cta_wide(st, jobs, njobs, o, kMaxCta, sub_log, sms, nullptr)
-             : inv_cta(st, jobs, njobs, o, kMaxCta, sub_log, sms, vkh_variant(2, kMaxCta));
+             : inv_cta(st, jobs, njobs, o, kMaxCta, sub_log, sms, vkh_variant_jobs(2, kMaxCta, (long)njobs << sub_log, sms));
     for (int p = global_passes((int)log_n) - 1; !e && p >= 0; p--) {
       int s0, kk;
       global_split((int)log_n, p, &s0, &kk);
@@ -333,8 +333,8 @@ extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int nj
   }
   if (split_small(njobs, log_n, sms)) return poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
   if (log_n <= (uint32_t)kMaxCta) {
-    if (lp) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n), *lift);
-    return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant(0, (int)log_n));
+    if (lp) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms), *lift);
+    return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms));
   }
   return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lp);
 }

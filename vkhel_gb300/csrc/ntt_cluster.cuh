@@ -64,9 +64,11 @@ __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.w
 // loads and butterflies run before the wait, which comes just before the
 // first remote store (the fused polymul: 1-2.4 % faster; the forward
 // transform alone was 0.8 % slower this way and synchronizes before).
+// rbase: the cluster rank of this transform's CTA 0 (a larger cluster can
+// hold several transforms of C CTAs each).
 template <int LOGC, class S, bool SPLIT>
 __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, const cg::cluster_group& cl, int rank,
-                                        const Tw& t) {
+                                        const Tw& t, int rbase = 0) {
   using K = Cols<LOGC, S>;
   constexpr int H = K::PER >= 2 ? K::PER / 2 : 1;
   const ulonglong2 w0 = ld_tw(t.fwd + 1);
@@ -87,7 +89,7 @@ __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, con
     if (SPLIT && k0 == 0) cluster_wait();
 #pragma unroll
     for (int j = 0; j < K::C; j++) {
-      u64* rem = cl.map_shared_rank(sm, j);
+      u64* rem = cl.map_shared_rank(sm, rbase + j);
 #pragma unroll
       for (int k = 0; k < H; k++) rem[pad(K::col(rank, k0 + k))] = v[k * K::C + j];
     }
@@ -98,7 +100,7 @@ __device__ __forceinline__ void col_fwd(const u64* __restrict__ in, u64* sm, con
 // canonical words to global memory; two rounds of H columns as above.
 template <int LOGC, class S, class Epi>
 __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
-                                        const Tw& t, const Epi& epi) {
+                                        const Tw& t, const Epi& epi, int rbase = 0) {
   using K = Cols<LOGC, S>;
   constexpr int H = K::PER >= 2 ? K::PER / 2 : 1;
 #pragma unroll 1
@@ -106,7 +108,7 @@ __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg
     u64 v[H * K::C];
 #pragma unroll
     for (int j = 0; j < K::C; j++) {
-      const u64* rem = cl.map_shared_rank(sm, j);
+      const u64* rem = cl.map_shared_rank(sm, rbase + j);
 #pragma unroll
       for (int k = 0; k < H; k++) v[k * K::C + j] = rem[pad(K::col(rank, k0 + k))];
     }
@@ -123,11 +125,11 @@ __device__ __forceinline__ void col_inv(u64* __restrict__ out, u64* sm, const cg
 
 template <int LOGC, class S, bool LIFT>
 __device__ __forceinline__ void col_inv_out(u64* __restrict__ out, u64* sm, const cg::cluster_group& cl, int rank,
-                                            const Tw& t, const vkcu_lift* lift) {
+                                            const Tw& t, const vkcu_lift* lift, int rbase = 0) {
   if constexpr (LIFT)
-    col_inv<LOGC, S>(out, sm, cl, rank, t, LiftRun(lift, t.q));
+    col_inv<LOGC, S>(out, sm, cl, rank, t, LiftRun(lift, t.q), rbase);
   else
-    col_inv<LOGC, S>(out, sm, cl, rank, t, NoLift{});
+    col_inv<LOGC, S>(out, sm, cl, rank, t, NoLift{}, rbase);
 }
 
 template <int LOGC, class S>

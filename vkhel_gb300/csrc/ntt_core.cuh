@@ -332,9 +332,12 @@ __device__ __forceinline__ void gs_group(u64 (&v)[NV], const ulonglong2* tw, u32
 // a direction share one loop body (the stage offset is a runtime value), and
 // the fused polymul runs its two forward transforms through the same code.
 
-template <int LOGN_, int E_, int U_ = 1, class M_ = Mod62>
+template <int LOGN_, int E_, int U_ = 1, class M_ = Mod62, bool DUAL_ = false>
 struct Shape {
   using M = M_;  // modulus class
+  // DUAL: the CTA holds 2 T threads running two transforms of this shape in
+  // step, thread t on the one of half t / T (shared barriers, separate words)
+  static constexpr bool DUAL = DUAL_;
   static constexpr int LOGN = LOGN_, E = E_;
   static constexpr int U = U_;  // radix-16 groups of a thread in flight at once (1 or 2)
   static constexpr int N = 1 << LOGN, T = N / E;
@@ -342,6 +345,8 @@ struct Shape {
   static constexpr int FIRSTK = HEAD % 4 == 0 ? 4 : HEAD % 4;
   static constexpr int SMEM_BYTES = (N + N / 16) * 8;
   static_assert(E >= 16 && (E % 16) == 0 && HEAD >= 1 && T >= 1, "unsupported shape");
+  // this thread's index within its transform
+  __device__ __forceinline__ static int tid() { return DUAL ? (int)(threadIdx.x & (T - 1)) : (int)threadIdx.x; }
 };
 
 // A radix-16 pass starting at stage s0 of an n = 2^logn transform: group g
@@ -380,7 +385,7 @@ __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, c
     for (int i = 0; i < GR; i++)
 #pragma unroll
       for (int j = 0; j < (1 << KK); j++)
-        v[i * (1 << KK) + j] = ld_stream(in + (int)threadIdx.x + (i0 + i) * S::T + j * TMIN);
+        v[i * (1 << KK) + j] = ld_stream(in + S::tid() + (i0 + i) * S::T + j * TMIN);
     const ulonglong2 w0 = ld_tw(t.fwd + tw_mult);
     static_for<0, GR>([&](auto ic) {
       constexpr int i = decltype(ic)::value;
@@ -388,7 +393,7 @@ __device__ __forceinline__ void fwd_first(u64* sm, const u64* __restrict__ in, c
       for (int jj = 0; jj < (1 << (KK - 1)); jj++)
         ct_first<typename S::M>(v[i * (1 << KK) + jj], v[i * (1 << KK) + jj + (1 << (KK - 1))], w0.x, w0.y, t);
       ct_group<typename S::M, KK, 1, i * (1 << KK)>(v, t.fwd, tw_mult, t);
-      const int g = (int)threadIdx.x + (i0 + i) * S::T;
+      const int g = S::tid() + (i0 + i) * S::T;
 #pragma unroll
       for (int j = 0; j < (1 << KK); j++) sm[pad(g + j * TMIN)] = v[i * (1 << KK) + j];
     });
@@ -403,7 +408,7 @@ __device__ __forceinline__ void fwd_first_smem(u64* sm, const Tw& t, u32 tw_mult
   constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK, GR = round_groups<KK, G>();
 #pragma unroll 1
   for (int i0 = 0; i0 < G; i0 += GR) {
-    const int g0 = (int)threadIdx.x + i0 * S::T;
+    const int g0 = S::tid() + i0 * S::T;
     u64 v[GR << KK];
 #pragma unroll
     for (int i = 0; i < GR; i++)
@@ -430,7 +435,7 @@ __device__ __forceinline__ void fwd_passes(u64* sm, const Tw& t, u32 tw_mult, Ep
     const int st = 1 << ps.lt;
 #pragma unroll(S::U)
     for (int i = 0; i < S::E / 16; i++) {
-      const int g = (int)threadIdx.x + i * S::T;
+      const int g = S::tid() + i * S::T;
       const int a0 = ps.first(g);
       u64 v[16];
 #pragma unroll
@@ -457,7 +462,7 @@ __device__ __forceinline__ void inv_passes(u64* sm, const Tw& t, u32 tw_mult, in
     const int st = 1 << ps.lt;
 #pragma unroll(S::U)
     for (int i = 0; i < S::E / 16; i++) {
-      const int g = (int)threadIdx.x + i * S::T;
+      const int g = S::tid() + i * S::T;
       const int a0 = ps.first(g);
       u64 v[16];
 #pragma unroll
@@ -477,7 +482,7 @@ __device__ __forceinline__ void inv_last_smem(u64* sm, const Tw& t, u32 tw_mult)
   constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK, GR = round_groups<KK, G>();
 #pragma unroll 1
   for (int i0 = 0; i0 < G; i0 += GR) {
-    const int g0 = (int)threadIdx.x + i0 * S::T;
+    const int g0 = S::tid() + i0 * S::T;
     u64 v[GR << KK];
 #pragma unroll
     for (int i = 0; i < GR; i++)
@@ -540,7 +545,7 @@ __device__ __forceinline__ void inv_last_epi(u64* sm, const Tw& t, u32 tw_mult, 
   constexpr int KK = S::FIRSTK, G = S::E >> KK, TMIN = S::N >> KK;
 #pragma unroll 1
   for (int i = 0; i < G; i++) {
-    const int g = (int)threadIdx.x + i * S::T;
+    const int g = S::tid() + i * S::T;
     u64 v[1 << KK];
 #pragma unroll
     for (int j = 0; j < (1 << KK); j++) v[j] = sm[pad(g + j * TMIN)];

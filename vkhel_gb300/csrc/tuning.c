@@ -1,14 +1,19 @@
 /*
  * Kernel variant table (the autotuner's output).
  *
- * For every kernel family and degree the table names the variant the
- * dispatcher launches; vkhel_gb300/autotune.py measures the variants on the
- * GPU and writes the table as text, one "family log_n variant" triple per line
- * ('#' starts a comment).  The table is read once per process from
- * $VKHEL_TUNE_TABLE, or, when that is unset, from tuning/gb300.txt beside the
- * package that holds libvkhel.so (found through dladdr).  Missing entries keep
- * the built-in default, variant 0.  vkhel_tune_set changes an entry at run
- * time (the autotuner uses it to try each variant).
+ * For every kernel family, degree and job-count bucket the table names the
+ * variant the dispatcher launches; vkhel_gb300/autotune.py measures the
+ * variants on the GPU and writes the table as text, one "family log_n
+ * variant [bucket]" line per entry ('#' starts a comment).  The bucket is the
+ * launch's jobs per SM: 0 for at most 1, 1 for at most 2, 2 for at most 4, 3
+ * for more (the shapes differ in threads per CTA and so in CTAs per SM, and
+ * the job count of a degree class -- instances times limbs -- decides how the
+ * last wave fills); a line without a bucket sets all four.  The table is read
+ * once per process from $VKHEL_TUNE_TABLE, or, when that is unset, from
+ * tuning/gb300.txt beside the package that holds libvkhel.so (found through
+ * dladdr).  Missing entries keep the built-in default, variant 0.
+ * vkhel_tune_set changes an entry (all buckets) at run time (the autotuner
+ * uses it to try each variant).
  */
 #define _GNU_SOURCE
 #include <dlfcn.h>
@@ -21,8 +26,9 @@
 
 #define FAMILIES 4
 #define DEGREES 32
+#define BUCKETS 4
 
-static int g_table[FAMILIES][DEGREES];
+static int g_table[FAMILIES][DEGREES][BUCKETS];
 static pthread_once_t g_once = PTHREAD_ONCE_INIT;
 static pthread_mutex_t g_mu = PTHREAD_MUTEX_INITIALIZER;
 
@@ -36,10 +42,15 @@ static int load_file(const char *path) {
 		char *hash = strchr(line, '#');
 		if (hash)
 			*hash = 0;
-		unsigned fam, log_n;
+		unsigned fam, log_n, bucket;
 		int var;
-		if (sscanf(line, "%u %u %d", &fam, &log_n, &var) == 3 && fam < FAMILIES && log_n < DEGREES && var >= 0) {
-			g_table[fam][log_n] = var;
+		const int got = sscanf(line, "%u %u %d %u", &fam, &log_n, &var, &bucket);
+		if (got >= 3 && fam < FAMILIES && log_n < DEGREES && var >= 0) {
+			if (got == 4 && bucket >= BUCKETS)
+				continue;
+			for (unsigned b = 0; b < BUCKETS; b++)
+				if (got == 3 || b == bucket)
+					g_table[fam][log_n][b] = var;
 			n++;
 		}
 	}
@@ -72,14 +83,24 @@ static void init_table(void) {
 	load_file(path);
 }
 
-int vkh_variant(int family, int log_n) {
+static int bucket_of(long njobs, int sms) {
+	const long s = sms > 0 ? sms : 1;
+	return njobs <= s ? 0 : njobs <= 2 * s ? 1 : njobs <= 4 * s ? 2 : 3;
+}
+
+int vkh_variant_jobs(int family, int log_n, long njobs, int sms) {
 	pthread_once(&g_once, init_table);
 	if (family < 0 || family >= FAMILIES || log_n < 0 || log_n >= DEGREES)
 		return 0;
 	pthread_mutex_lock(&g_mu);
-	const int v = g_table[family][log_n];
+	const int v = g_table[family][log_n][bucket_of(njobs, sms)];
 	pthread_mutex_unlock(&g_mu);
 	return v;
+}
+
+/* The entry for many jobs (more than 4 per SM), and the flags of family 3. */
+int vkh_variant(int family, int log_n) {
+	return vkh_variant_jobs(family, log_n, 1L << 40, 1);
 }
 
 int vkhel_tune_set(uint32_t family, uint32_t log_n, int32_t variant) {
@@ -87,7 +108,8 @@ int vkhel_tune_set(uint32_t family, uint32_t log_n, int32_t variant) {
 	if (family >= FAMILIES || log_n >= DEGREES || variant < 0)
 		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "tune_set: bad family/log_n/variant");
 	pthread_mutex_lock(&g_mu);
-	g_table[family][log_n] = variant;
+	for (int b = 0; b < BUCKETS; b++)
+		g_table[family][log_n][b] = variant;
 	pthread_mutex_unlock(&g_mu);
 	return VKHEL_OK;
 }
