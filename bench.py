@@ -262,8 +262,11 @@ def serving_sweep(vk, torch, orc, rates=(1000, 4000, 16000, None), seconds=1.0, 
                        "pinned host operands; 40 GB device budget",
            "rates": []}
     with vk.Server(device_budget=40 << 30, max_batch_limbs=512, max_inflight_batches=3) as srv:
-        for p_ in pay:  # warm-up: table uploads, pool growth
+        for p_ in pay:  # warm-up: table uploads
             srv.wait(srv.submit(p_[2], p_[3], p_[4], p_[5]))
+        for _ in range(2):  # and the device pool grown to what many requests in flight hold
+            for r in [srv.submit(p_[2], p_[3], p_[4], p_[5]) for p_ in pay]:
+                srv.wait(r)
         for rate in rates:
             count = int(min(6000, (rate or 20000) * seconds)) if rate else 2000
             gaps = rng.exponential(1.0 / rate, size=count) if rate else np.zeros(count)
@@ -681,8 +684,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving sweep")
     ap.add_argument("--profile", action="store_true",
                     help="small profiling case: build the batch, launch it --steps times, print nothing else")
-    ap.add_argument("--extra", choices=sorted(EXTRAS),
-                    help="run one of the secondary measurements alone and print its JSON (profiling aid)")
+    ap.add_argument("--extra", choices=sorted(EXTRAS) + ["serving"],
+                    help="run one of the secondary measurements (or the serving sweep) alone and print its JSON")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -699,6 +702,9 @@ def main():
     import vkhel_gb300 as vk
     from oracle import pyoracle
     from vkhel_gb300 import workloads
+    if args.extra == "serving":
+        print(json.dumps({"serving": serving_sweep(vk, torch, pyoracle.load())}), flush=True)
+        return
     if args.extra:
         ctx = vk.Context()
         print(json.dumps({args.extra: EXTRAS[args.extra](vk, ctx, torch, pyoracle.load())}), flush=True)

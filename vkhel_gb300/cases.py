@@ -18,6 +18,8 @@ the device so that a profiler capture of one launch ends quickly.
   pointwise     32 polymuls of n = 2^18 (composed path)         k_pointwise
   simple        4096 forward + inverse transforms of n = 2^7    k_ntt_fwd_simple, k_ntt_inv_simple
   wide_polymul  256 polymuls of n = 2^14, 63-bit primes         k_polymul<14,..,Mod63>
+  cluster_polymul  64 polymuls of n = 2^16 (single-limb batch)  k_polymul_cluster<2,..>
+  ragged_single  256 ragged instances, n = 2^12..2^16, as one launch   k_polymul_ragged
   elementwise   elemgtsub / elemmod / elemgtadd / elemfma on 2^25 words   k_elementwise<...>
 """
 import argparse
@@ -111,6 +113,25 @@ def case_simple(ctx):
 
 def case_wide_polymul(ctx):
     return _polymul_batch(ctx, 1 << 14, 256, bits=63)
+
+
+def case_cluster_polymul(ctx):
+    return _polymul_batch(ctx, 1 << 16, 64, primes=1)
+
+
+def case_ragged_single(ctx):
+    inst = workloads.ragged_batch(256, seed=33)
+    tabs, keep = {}, []
+    vk.lib().vkhel_tune_set(3, 2, 1)  # the single-launch form for this process
+    bt = vk.Batch(ctx)
+    for n, qs, ws, a, b in inst:
+        for q, w in zip(qs, ws):
+            tabs.setdefault((n, q), vk.NttTables(n, q, w))
+        va, vb, vc = vk.Vector(ctx, a), vk.Vector(ctx, b), vk.Vector(ctx, len(qs) * n)
+        bt.add_polymul([tabs[(n, q)] for q in qs], va, vb, vc)
+        keep.append((va, vb, vc))
+    bt.commit(graph=True)
+    return bt.launch, (bt, keep, tabs)
 
 
 def case_elementwise(ctx):

@@ -160,23 +160,28 @@ __device__ __forceinline__ u64 shoup_factor(u64 r, u64 q) {
   return (u64)((((unsigned __int128)r) << 64) / q);
 }
 
+// Thread s writes slot s of both tables, so the 16-byte pairs of consecutive
+// threads are contiguous (whole sectors, no read-modify-write in L2):
+// fwd[s] = w^j with j = bitrev(s) (the reference's roots[bitrev(j)] = w^j),
+// inv[s] = q - w^(n - j) = w^-j for s > 0 (the index rule for w^n = -1) and
+// inv[0] = 1.
+__device__ __forceinline__ u64 power_of(const u64* __restrict__ phi, const u64* __restrict__ plo, u64 i, u32 lb, u64 q,
+                                        u64 mu, u32 qbits) {
+  const u64 x = phi[i >> lb], y = plo[i & ((1ull << lb) - 1)];
+  return ref_reduce128(mulhi(x, y), x * y, q, mu, qbits);
+}
+
 __global__ void k_twiddles(u64* __restrict__ fwd, u64* __restrict__ inv, const u64* __restrict__ phi,
                            const u64* __restrict__ plo, u32 log_n, u32 lb, u64 q, u64 mu, u32 qbits) {
   const u64 n = 1ull << log_n;
-  for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
-    const u64 x = phi[i >> lb], y = plo[i & ((1ull << lb) - 1)];
-    const u64 p = i == 0 ? 1ull : ref_reduce128(mulhi(x, y), x * y, q, mu, qbits);
-    const u32 s = __brev((u32)i) >> (32 - log_n);
+  for (u64 s = (u64)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (u64)gridDim.x * blockDim.x) {
+    const u64 j = __brev((u32)s) >> (32 - log_n);
+    const u64 p = j == 0 ? 1ull : power_of(phi, plo, j, lb, q, mu, qbits);
+    const u64 r = s == 0 ? 1ull : q - power_of(phi, plo, n - j, lb, q, mu, qbits);
     fwd[2 * s] = p;
     fwd[2 * s + 1] = shoup_factor(p, q);
-    if (i == 0) {
-      inv[0] = 1;
-      inv[1] = shoup_factor(1, q);
-    } else {
-      const u32 s2 = __brev((u32)(n - i)) >> (32 - log_n);
-      inv[2 * s2] = q - p;
-      inv[2 * s2 + 1] = shoup_factor(q - p, q);
-    }
+    inv[2 * s] = r;
+    inv[2 * s + 1] = shoup_factor(r, q);
   }
 }
 
