@@ -963,6 +963,11 @@ def main():
         "batch_latency_ms_p50": statistics.median(iso_ms),
         "batch_latency_ms_p99": pct(iso_ms, 0.99),
     }
+    # the headline's contexts, batches and pinned buffers are done with: free
+    # them before the secondary measurements run
+    del sets, e2e_sets, pins
+    for c in ctxs:
+        c.close()
     if rank == 0 and not args.no_serve:
         result["serving"] = serving_sweep(vk, torch, orc)
         result.update(extra_configs(vk, torch))
@@ -972,8 +977,6 @@ def main():
         print(json.dumps(result), flush=True)
     if dist:
         dist.destroy_process_group()
-    for c in ctxs:
-        c.close()
 
 
 if __name__ == "__main__":

@@ -9,10 +9,11 @@ asking the context's pool for it.  This test calls it through the C ABI twice
 in a row, on a fresh context whose budget is frozen at the bytes already in
 use (so any pool allocation would fail), and checks each result bit for bit
 against the allocating entry point vkhel_vector_polymul and against the CPU
-oracle's polymul, for a 60-bit prime and for the largest NTT prime below
-2^62 (the top of the kernel's modulus range).  The tolerance is zero: the
-products are integer arithmetic.  The file is named to be collected last and
-uses only its own context, so it passes alone or after the rest of the suite.
+oracle's polymul, for a 60-bit prime and for the largest NTT primes below
+2^62 and below 2^63 (the top of each of the two kernel families' ranges).
+The tolerance is zero: the products are integer arithmetic.  The file is
+named to be collected last and uses only its own context, so it passes alone
+or after the rest of the suite.
 """
 import numpy as np
 import pytest
@@ -22,7 +23,7 @@ from vkhel_gb300 import workloads
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("qbound", [1 << 60, 1 << 62])
+@pytest.mark.parametrize("qbound", [1 << 60, 1 << 62, 1 << 63])
 @pytest.mark.parametrize("log_n", [8, 12, 14])
 def test_noalloc_polymul_equals_allocating_polymul(vk, oracle, log_n, qbound):
     n = 1 << log_n
