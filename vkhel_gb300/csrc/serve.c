@@ -178,6 +178,9 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 		const int wide = (int) ((keys[i] >> 39) & 1);
 		sl->host_poly[i] = tmp[keys[i] & 0x7fffffffffull];
 		if (nclasses == 0 || classes[nclasses - 1].log_n != log_n || classes[nclasses - 1].wide != wide) {
+			/* at most two classes per degree 2^1 .. 2^26: 52 */
+			if (nclasses == SRV_MAX_CLASSES)
+				return VKHEL_ERR_UNSUPPORTED;
 			struct vkh_job_class *cl = &classes[nclasses++];
 			cl->kind = VKH_JOB_POLYMUL;
 			cl->log_n = log_n;
