@@ -21,6 +21,10 @@ the device so that a profiler capture of one launch ends quickly.
   cluster_polymul  64 polymuls of n = 2^16 (single-limb batch)  k_polymul_cluster<2,..>
   ragged_single  256 ragged instances, n = 2^12..2^16, as one launch   k_polymul_ragged
   elementwise   elemgtsub / elemmod / elemgtadd / elemfma on 2^25 words   k_elementwise<...>
+  elementwise_rest  elemmod mod 2, elemfma_canonical, the n^-1 scaling and lift of
+                the words past n of an inverse transform      k_elementwise<...>, k_lift_range
+  wide_transforms  1024 forward transforms of n = 2^14 and 64 of n = 2^16, 63-bit primes
+                k_ntt_fwd<14,..,Mod63>, k_ntt_fwd_cluster<2, Shape<14,32,1,Mod63>>
 """
 import argparse
 import sys
@@ -148,6 +152,43 @@ def case_elementwise(ctx):
         vk.elemgtadd(a, r, q // 2, 17)
         vk.elemfma(a, b, r, 12345, q)
     return run, (a, b, r)
+
+
+def case_elementwise_rest(ctx):
+    words = 1 << 25
+    q = (1 << 61) - 1
+    rng = np.random.default_rng(9)
+    a = vk.Vector(ctx, workloads.uniform(rng, q, words))
+    b = vk.Vector(ctx, workloads.uniform(rng, q, words))
+    r = vk.Vector(ctx, words)
+    n = 1 << 14
+    qq = workloads.ntt_primes(n, 1)[0]
+    t = vk.NttTables(n, qq, workloads.root_for(n, qq))
+    long_in = vk.Vector(ctx, workloads.uniform(rng, qq, words))
+
+    def run():
+        vk.elemmod(a, r, 2, q)                  # OpModTwo
+        vk.elemfma_canonical(a, b, r, 12345, q)  # OpFmaCanon
+        # an inverse transform into a vector of 2^25 words: the words past n
+        # are scaled by n^-1 (OpMulConst) and lifted (k_lift_range)
+        vk.inverse_transform_lift(long_in, r, t, [("elemmod", 65537, 0)])
+    return run, (a, b, r, t, long_in)
+
+
+def case_wide_transforms(ctx):
+    f14, k14 = _wide_transform_batch(ctx, 1 << 14, 1024)
+    f16, k16 = _wide_transform_batch(ctx, 1 << 16, 64)
+    return (lambda: (f14(), f16())), (k14, k16)
+
+
+def _wide_transform_batch(ctx, n, jobs, primes=8):
+    qs, tabs = _tabs(n, primes, bits=63)
+    x = _operands(ctx, n, qs, jobs, n + jobs)
+    y = vk.Vector(ctx, jobs * n)
+    bt = vk.Batch(ctx)
+    bt.add_transform([tabs[j % primes] for j in range(jobs)], x, y)
+    bt.commit(graph=True)
+    return bt.launch, (bt, x, y, tabs)
 
 
 CASES = {k[5:]: v for k, v in globals().items() if k.startswith("case_")}
