@@ -75,6 +75,46 @@ def test_batch_commit_failure_then_fresh_batch(vk, ctx, oracle):
     np.testing.assert_array_equal(c.download(), oracle.polymul(a_h, b_h, n, q, w)[0])
 
 
+def test_batch_commit_retried_after_a_failure(vk, oracle):
+    """A commit that fails part-way (here the single-launch item table, after
+    the job table was allocated) leaves the batch uncommitted; committing it
+    again succeeds, computes the right words and frees everything the first
+    attempt had taken."""
+    L = vk.lib()
+    saved = L.vkhel_tune_get(3, 2)
+    L.vkhel_tune_set(3, 2, 1)
+    try:
+        with vk.Context() as fresh:
+            shapes = [(1 << 12, 1), (1 << 14, 2)]
+            tabs, vecs, refs = [], [], []
+            for n, k in shapes:
+                q, w, a_h, b_h = _operands(n, k)
+                t = vk.NttTables(n, q, w)
+                a, b, c = vk.Vector(fresh, a_h), vk.Vector(fresh, b_h), vk.Vector(fresh, n)
+                tabs.append(t)
+                vecs.append((a, b, c))
+                refs.append(oracle.polymul(a_h, b_h, n, q, w)[0])
+            before = fresh.bytes_in_use
+            bt = vk.Batch(fresh)
+            for t, (a, b, c) in zip(tabs, vecs):
+                bt.add_polymul([t], a, b, c)
+            vk.fail_allocations(1, 1)       # the job table succeeds, the item table fails
+            with pytest.raises(vk.VkhelError) as e:
+                bt.commit(graph=True)
+            assert e.value.code == OOM
+            bt.commit(graph=True)
+            bt.run()
+            assert bt.kernels == 1
+            for (a, b, c), ref in zip(vecs, refs):
+                np.testing.assert_array_equal(c.download(), ref)
+            bt.close()
+            fresh.sync()
+            assert fresh.bytes_in_use == before
+    finally:
+        vk.fail_allocations(0, 0)
+        L.vkhel_tune_set(3, 2, saved)
+
+
 def test_table_upload_failure_then_success(vk, oracle):
     n = 1 << 10
     q, w, a_h, _ = _operands(n, 2)

@@ -343,6 +343,11 @@ static int issue(struct vkhel_batch *b) {
  * that writes a dummy buffer. */
 static int ragged_setup(struct vkhel_batch *b) {
 	b->ragged = 0;
+	if (b->ragged_dev) { /* a commit that failed after this step is being retried */
+		vkh_dev_free(b->ctx, b->ragged_dev, b->ragged_bytes);
+		b->ragged_dev = NULL;
+		b->ragged_bytes = 0;
+	}
 	if (b->nclasses < 2 || vkh_variant(3, 2) != 1)
 		return VKHEL_OK;
 	uint32_t first[17] = {0}, count[17] = {0};
@@ -422,6 +427,20 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_commit: already committed");
 	if (b->njobs == 0)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_commit: empty batch");
+	/* what a commit that failed part-way left behind (retried commit) */
+	vkcu_graph_destroy(b->graph);
+	b->graph = NULL;
+	for (uint32_t k = 0; k < b->naux; k++) {
+		vkcu_stream_destroy(b->aux[k]);
+		vkcu_event_destroy(b->join[k]);
+	}
+	b->naux = 0;
+	vkcu_event_destroy(b->fork);
+	b->fork = NULL;
+	vkh_dev_free(ctx, b->dev, b->dev_bytes);
+	vkh_dev_free(ctx, b->scratch, b->scratch_bytes);
+	b->dev = b->scratch = NULL;
+	b->dev_bytes = b->scratch_bytes = 0;
 	qsort(b->recs, b->njobs, sizeof(*b->recs), cmp_rec);
 
 	/* classes and scratch slices */
