@@ -94,10 +94,10 @@ def test_batch_commit_retried_after_a_failure(vk, oracle):
                 tabs.append(t)
                 vecs.append((a, b, c))
                 refs.append(oracle.polymul(a_h, b_h, n, q, w)[0])
-            before = fresh.bytes_in_use
             bt = vk.Batch(fresh)
             for t, (a, b, c) in zip(tabs, vecs):
                 bt.add_polymul([t], a, b, c)
+            before = fresh.bytes_in_use     # the adds made the tables resident
             vk.fail_allocations(1, 1)       # the job table succeeds, the item table fails
             with pytest.raises(vk.VkhelError) as e:
                 bt.commit(graph=True)
