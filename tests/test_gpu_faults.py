@@ -75,6 +75,36 @@ def test_batch_commit_failure_then_fresh_batch(vk, ctx, oracle):
     np.testing.assert_array_equal(c.download(), oracle.polymul(a_h, b_h, n, q, w)[0])
 
 
+def test_failed_batch_add_records_nothing(vk, oracle):
+    """An add whose second limb's tables cannot be made resident fails as a
+    whole: the batch keeps none of that call's jobs, and the same add then
+    succeeds and computes the right words."""
+    n = 1 << 12
+    qs = workloads.ntt_primes(n, 2)
+    tabs = [vk.NttTables(n, q, workloads.root_for(n, q)) for q in qs]
+    rng = np.random.default_rng(5)
+    a_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+    b_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+    with vk.Context() as fresh:
+        a, b, c = vk.Vector(fresh, a_h), vk.Vector(fresh, b_h), vk.Vector(fresh, 2 * n)
+        bt = vk.Batch(fresh)
+        vk.fail_allocations(1, 1)           # limb 0's tables upload, limb 1's fail
+        with pytest.raises(vk.VkhelError) as e:
+            bt.add_polymul(tabs, a, b, c)
+        assert e.value.code == OOM
+        assert bt.jobs == 0
+        bt.add_polymul(tabs, a, b, c)
+        assert bt.jobs == 2
+        bt.commit()
+        bt.run()
+        got = c.download()
+        for k, q in enumerate(qs):
+            w = workloads.root_for(n, q)
+            want = oracle.polymul(a_h[k * n:(k + 1) * n], b_h[k * n:(k + 1) * n], n, q, w)[0]
+            np.testing.assert_array_equal(got[k * n:(k + 1) * n], want)
+        bt.close()
+
+
 def test_batch_commit_retried_after_a_failure(vk, oracle):
     """A commit that fails part-way (here the single-launch item table, after
     the job table was allocated) leaves the batch uncommitted; committing it
@@ -113,6 +143,29 @@ def test_batch_commit_retried_after_a_failure(vk, oracle):
     finally:
         vk.fail_allocations(0, 0)
         L.vkhel_tune_set(3, 2, saved)
+
+
+def test_elem_batch_commit_retried_after_a_failure(vk, oracle):
+    """An element-wise batch whose unit-table allocation fails commits on the
+    second try, computes the oracle's words and frees what it took."""
+    q = workloads.ntt_primes(1 << 10, 1)[0]
+    rng = np.random.default_rng(9)
+    with vk.Context() as fresh:
+        a_h, b_h = workloads.uniform(rng, q, 5000), workloads.uniform(rng, q, 5000)
+        a, b, r = vk.Vector(fresh, a_h), vk.Vector(fresh, b_h), vk.Vector(fresh, 5000)
+        before = fresh.bytes_in_use
+        eb = vk.ElemBatch(fresh)
+        eb.add("elemmul", a, b, r, q)
+        vk.fail_allocations(0, 1)
+        with pytest.raises(vk.VkhelError) as e:
+            eb.commit()
+        assert e.value.code == OOM
+        eb.commit()
+        eb.run()
+        np.testing.assert_array_equal(r.download(), oracle.elemmul(a_h, b_h, q))
+        eb.close()
+        fresh.sync()
+        assert fresh.bytes_in_use == before
 
 
 def test_table_upload_failure_then_success(vk, oracle):

@@ -132,6 +132,14 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		b->recs = r;
 		b->cap = cap;
 	}
+	/* every limb's tables resident before any job is recorded, so a failed
+	 * add leaves the batch as it was (the lookups below are then hits) */
+	for (uint32_t k = 0; k < limbs; k++) {
+		const struct vkh_devtab *d = NULL;
+		const int st = vkh_devtab_get(ctx, tables[k], &d);
+		if (st)
+			return st;
+	}
 	for (uint32_t k = 0; k < limbs; k++) {
 		const struct vkh_devtab *d = NULL;
 		const int st = vkh_devtab_get(ctx, tables[k], &d);

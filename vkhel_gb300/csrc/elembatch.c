@@ -223,13 +223,19 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 	if (dep)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT,
 				"elem_batch_commit: job %u overlaps memory another job writes", bad);
+	/* what a commit that failed part-way left behind (retried commit) */
+	vkcu_graph_destroy(b->graph);
+	b->graph = NULL;
+	vkh_dev_free(ctx, b->dev, b->dev_bytes);
+	b->dev = NULL;
+	b->dev_bytes = 0;
 	uint64_t chunks = 0;
 	for (uint32_t i = 0; i < b->njobs; i++) {
 		const uint64_t unit = b->jobs[i].b ? VKCU_ELEM_CHUNK : VKCU_ELEM_CHUNK_UNARY;
 		chunks += (b->jobs[i].len + unit - 1) / unit;
 	}
-	b->dev_bytes = sizeof(vkcu_elem_job) * (chunks ? chunks : 1);
-	vkcu_elem_job *host = malloc(b->dev_bytes);
+	const uint64_t dev_bytes = sizeof(vkcu_elem_job) * (chunks ? chunks : 1);
+	vkcu_elem_job *host = malloc(dev_bytes);
 	if (!host)
 		return vkh_fail(ctx, VKHEL_ERR_OUT_OF_MEMORY, "elem_batch_commit: host allocation failed");
 	uint64_t k = 0;
@@ -246,11 +252,12 @@ int vkhel_elem_batch_commit(struct vkhel_elem_batch *b, uint32_t flags) {
 		}
 	}
 	b->chunks = chunks;
-	int st = vkh_dev_alloc(ctx, b->dev_bytes, &b->dev);
+	int st = vkh_dev_alloc(ctx, dev_bytes, &b->dev);
 	if (st) {
 		free(host);
 		return st;
 	}
+	b->dev_bytes = dev_bytes;
 	int e = vkcu_h2d(ctx->stream, b->dev, host, b->dev_bytes);
 	if (!e)
 		e = vkcu_sync(ctx->stream);
