@@ -520,6 +520,103 @@ def lift_epilogue(vk, ctx, torch, orc, pairs=4 * PAIRS):
             "epilogue_cost_frac": 1 - rates["lift"] / rates["plain"]}
 
 
+def ntt_operand_batch(vk, ctx, torch, orc, pairs=4 * PAIRS):
+    """The rns_batch polynomials (n = 16384, 8 limbs, seed 2) with b given in
+    the transform domain (vkhel_batch_add_polymul_ntt: NTT(b) made once by a
+    forward-transform batch and kept, as a key or plaintext is): device rate
+    against the plain batch (128 pairs, operands above L2), and end to end
+    through the public API at the headline's 32 pairs with pinned host
+    buffers -- a up, c down, NTT(b) resident -- steps rotating over four
+    contexts as the headline's e2e does.  Every limb product is checked
+    against the oracle's polymul of a and b."""
+    import time
+    from vkhel_gb300 import workloads
+    qs, ws, a, b = workloads.rns_batch(N, LIMBS, pairs, SEED)
+    tabs = [vk.NttTables(N, q, w) for q, w in zip(qs, ws)]
+    pa = [vk.Vector(ctx, a[i].reshape(-1)) for i in range(pairs)]
+    pb = [vk.Vector(ctx, b[i].reshape(-1)) for i in range(pairs)]
+    pn = [vk.Vector(ctx, LIMBS * N) for _ in range(pairs)]
+    pc = [vk.Vector(ctx, LIMBS * N) for _ in range(pairs)]
+    ft = vk.Batch(ctx)  # NTT(b), once
+    for i in range(pairs):
+        ft.add_transform(tabs, pb[i], pn[i])
+    ft.commit(graph=False)
+    ft.run()
+    ft.close()
+    rates = {}
+    for name, pre in (("plain", False), ("ntt_operand", True)):
+        bt = vk.Batch(ctx)
+        for i in range(pairs):
+            bt.add_polymul(tabs, pa[i], pn[i] if pre else pb[i], pc[i], b_ntt=pre)
+        bt.commit(graph=True)
+        rates[name] = pairs * LIMBS / _event_time(torch, ctx, bt.launch, 20)
+        bt.close()
+    pidx = np.tile(np.arange(LIMBS, dtype=np.uint32), pairs)
+    ref, _ = orc.polymul_batch(a.reshape(-1, N), b.reshape(-1, N), N, qs, ws, pidx,
+                               tables=orc.batch_tables(N, qs, ws))
+    got = np.stack([v.download().reshape(-1, N) for v in pc]).reshape(-1, N)
+    assert np.array_equal(got, ref), "NTT-operand batch differs from the oracle"
+    del pa, pb, pc
+
+    # end to end at 32 pairs: per step upload a, launch, download c
+    words = PAIRS * LIMBS * N
+    a32 = np.ascontiguousarray(a[:PAIRS]).reshape(-1)
+    ctxs, sets, pins = [vk.Context() for _ in range(E2E_CTX)], [], []
+    for c in ctxs:
+        tb = [vk.NttTables(N, q, w) for q, w in zip(qs, ws)]
+        va, vb, vn, vc = vk.Vector(c, words), vk.Vector(c, b[:PAIRS].reshape(-1)), vk.Vector(c, words), \
+            vk.Vector(c, words)
+        f = vk.Batch(c)
+        f.add_transform(tb * PAIRS, vb, vn)  # limb k of the 256 with the tables of prime k mod 8
+        f.commit(graph=False)
+        f.run()
+        f.close()
+        bt = vk.Batch(c)
+        for i in range(PAIRS):
+            off = 8 * i * LIMBS * N
+            bt.add_polymul(tb, va.device_ptr + off, vn.device_ptr + off, vc.device_ptr + off, b_ntt=True)
+        bt.commit(graph=True)
+        sets.append((c, va, vb, vn, vc, bt, tb))
+        pins.append((torch.from_numpy(a32.view(np.int64)).pin_memory(), torch.empty(words, dtype=torch.int64).pin_memory()))
+    L = vk.lib()
+
+    def step(k):
+        c, va, _, _, vc, bt, _ = sets[k % E2E_CTX]
+        ph_a, ph_c = pins[k % E2E_CTX]
+        L.vkhel_vector_upload_async(va.ptr, ph_a.data_ptr(), words)
+        bt.launch()
+        L.vkhel_vector_download_async(vc.ptr, ph_c.data_ptr(), words)
+
+    for k in range(2 * E2E_CTX):
+        step(k)
+    for c in ctxs:
+        c.sync()
+    steps = 200
+    t0 = time.perf_counter()
+    for k in range(steps):
+        step(k)
+    for c in ctxs:
+        c.sync()
+    e2e_s = (time.perf_counter() - t0) / steps
+    ref32 = ref[: PAIRS * LIMBS]
+    for k in range(E2E_CTX):
+        assert np.array_equal(pins[k][1].numpy().view(np.uint64).reshape(-1, N), ref32), \
+            "NTT-operand e2e differs from the oracle"
+    for s_ in sets:
+        s_[5].close()
+    del sets, pins
+    for c in ctxs:
+        c.close()
+    return {"workload": f"n={N}, {LIMBS} limbs, seed {SEED}; b given as NTT(b) (a forward-transform batch, once)",
+            "limb_polymul_per_s_plain": rates["plain"], "limb_polymul_per_s_ntt_operand": rates["ntt_operand"],
+            "device_pairs": pairs,
+            "e2e": {"value": PAIRS * LIMBS / e2e_s, "unit": UNIT, "ms_per_step": e2e_s * 1e3, "pairs": PAIRS,
+                    "h2d_bytes_per_step": 8 * words, "d2h_bytes_per_step": 8 * words,
+                    "path": "vkhel_vector_upload_async (a) + vkhel_batch_launch + vkhel_vector_download_async (c), "
+                            f"NTT(b) resident, pinned host buffers, steps rotating over {E2E_CTX} contexts"},
+            "checked_against_oracle": f"all {pairs * LIMBS} limb products (device) and the 256 of every context (e2e)"}
+
+
 def elementwise_batch(vk, ctx, torch, orc, jobs=2048, seed=6):
     """2048 ragged element-wise jobs (lengths uniform in 1 .. 2^17 words, ops
     cycling through elemfma, elemmul, elemmod, elemgtsub, elemgtadd, 61-bit
@@ -670,7 +767,8 @@ def transform_batch(vk, ctx, torch, orc, n=N, count=1024):
 EXTRAS = {"single_limb_batch": single_limb_batch, "ragged_batch": ragged_batch,
           "transform_batch": transform_batch,
           "standalone_ops": standalone_ops,
-          "lift_epilogue": lift_epilogue, "elementwise_batch": elementwise_batch,
+          "lift_epilogue": lift_epilogue, "ntt_operand_batch": ntt_operand_batch,
+          "elementwise_batch": elementwise_batch,
           "device_twiddles": device_twiddles}
 
 

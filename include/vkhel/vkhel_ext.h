@@ -103,6 +103,15 @@ void vkhel_vector_elemfma_canonical(const struct vkhel_vector *a,
 int vkhel_vector_polymul(const struct vkhel_vector *a,
 		const struct vkhel_vector *b, struct vkhel_vector *result,
 		struct vkhel_ntt_tables *ntt);
+/* The same product with b given in the transform domain: b_ntt holds NTT(b)
+ * as vkhel_vector_forward_transform writes it (bit-reversed order), e.g. a
+ * key or plaintext transformed once and reused.  Equal to the reference
+ * composition forward(a), elemmul(., b_ntt), inverse, so b_ntt's words need
+ * not be reduced (elemmul reduces its operands).  One transform fewer per
+ * product.  result may alias a, not b_ntt.  Returns a status. */
+int vkhel_vector_polymul_ntt(const struct vkhel_vector *a,
+		const struct vkhel_vector *b_ntt, struct vkhel_vector *result,
+		struct vkhel_ntt_tables *ntt);
 
 /* ---- centred-lift epilogues ----
  * Up to VKHEL_MAX_LIFT_STEPS of the reference's element-wise ops applied, in
@@ -177,6 +186,15 @@ int vkhel_batch_add_polymul(struct vkhel_batch *batch,
 int vkhel_batch_add_polymul_raw(struct vkhel_batch *batch,
 		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *b, uint64_t *c);
+/* Limb products with b in the transform domain (vkhel_vector_polymul_ntt):
+ * limb k of b_ntt holds NTT(b_k) for tables[k]; c must not overlap b_ntt. */
+int vkhel_batch_add_polymul_ntt(struct vkhel_batch *batch,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *a, const struct vkhel_vector *b_ntt,
+		struct vkhel_vector *c);
+int vkhel_batch_add_polymul_ntt_raw(struct vkhel_batch *batch,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b_ntt, uint64_t *c);
 /* Transforms of `limbs` limbs: limb k of `out` (n words at offset k n) =
  * the forward or inverse transform of limb k of `in` with tables[k], equal
  * to vkhel_vector_forward_transform / vkhel_vector_inverse_transform of that

@@ -73,11 +73,14 @@ _SIGNATURES = [
     ("vkhel_vector_elemfma_canonical", None, [vp, vp, vp, u64, u64]),
     ("vkhel_vector_polymul", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_vector_polymul_noalloc", ctypes.c_int, [vp, vp, vp, vp]),
+    ("vkhel_vector_polymul_ntt", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_vector_polymul_lift", ctypes.c_int, [vp, vp, vp, vp, vp, u32]),
     ("vkhel_vector_inverse_transform_lift", ctypes.c_int, [vp, vp, vp, vp, u32]),
     ("vkhel_batch_create", vp, [vp]),
     ("vkhel_batch_add_polymul", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_batch_add_polymul_ntt", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_batch_add_polymul_ntt_raw", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
     ("vkhel_batch_add_polymul_lift", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, vp, vp, u32]),
     ("vkhel_batch_add_transform", ctypes.c_int, [vp, ctypes.POINTER(vp), u32, vp, vp, u32, vp, u32]),
     ("vkhel_debug_fail_allocations", ctypes.c_int, [u64, u64]),
@@ -384,6 +387,11 @@ def polymul(a, b, res, tables):
     _status(res.ctx.ptr, lib().vkhel_vector_polymul(a.ptr, b.ptr, res.ptr, tables.ptr))
 
 
+def polymul_ntt(a, b_ntt, res, tables):
+    """vkhel_vector_polymul_ntt: the product with b given as NTT(b) (a forward transform's output)."""
+    _status(res.ctx.ptr, lib().vkhel_vector_polymul_ntt(a.ptr, b_ntt.ptr, res.ptr, tables.ptr))
+
+
 def polymul_noalloc(a, b, res, tables):
     """vkhel_vector_polymul_noalloc: same product, scratch in a static device array."""
     _status(res.ctx.ptr, lib().vkhel_vector_polymul_noalloc(a.ptr, b.ptr, res.ptr, tables.ptr))
@@ -443,10 +451,18 @@ class Batch:
         self._keep = []
         ctx._children.add(self)
 
-    def add_polymul(self, tables, a, b, c, lift=None):
+    def add_polymul(self, tables, a, b, c, lift=None, b_ntt=False):
+        """Limb products of a and b into c; b_ntt=True: b holds NTT(b) of every limb."""
         arr = (vp * len(tables))(*[t.ptr for t in tables])
         self._keep.append((tables, a, b, c))  # the batch reads and writes them at every launch
-        if lift:
+        if b_ntt:
+            if lift:
+                raise ValueError("b_ntt has no lift form")
+            if isinstance(a, Vector):
+                code = lib().vkhel_batch_add_polymul_ntt(self.ptr, arr, len(tables), a.ptr, b.ptr, c.ptr)
+            else:
+                code = lib().vkhel_batch_add_polymul_ntt_raw(self.ptr, arr, len(tables), int(a), int(b), int(c))
+        elif lift:
             steps, n = lift_steps(lift)
             code = lib().vkhel_batch_add_polymul_lift(self.ptr, arr, len(tables), a.ptr, b.ptr, c.ptr,
                                                       ctypes.addressof(steps), n)

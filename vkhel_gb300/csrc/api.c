@@ -607,12 +607,22 @@ int vkh_lift_compile(struct vkhel_ctx *ctx, const struct vkhel_lift_step *steps,
 }
 
 static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
-		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps);
+		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps, int b_ntt);
 
 int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t) {
 	vkcu_range_push("vkhel_vector_polymul");
-	const int st = polymul_impl(a, b, res, t, NULL, 0);
+	const int st = polymul_impl(a, b, res, t, NULL, 0, 0);
+	vkcu_range_pop();
+	return st;
+}
+
+/* The reference's call pattern forward(a), elemmul(., NTT(b)), inverse with
+ * NTT(b) kept from an earlier forward transform, in one call. */
+int vkhel_vector_polymul_ntt(const struct vkhel_vector *a, const struct vkhel_vector *b_ntt,
+		struct vkhel_vector *res, struct vkhel_ntt_tables *t) {
+	vkcu_range_push("vkhel_vector_polymul_ntt");
+	const int st = polymul_impl(a, b_ntt, res, t, NULL, 0, 1);
 	vkcu_range_pop();
 	return st;
 }
@@ -620,19 +630,22 @@ int vkhel_vector_polymul(const struct vkhel_vector *a, const struct vkhel_vector
 int vkhel_vector_polymul_lift(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
 		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
 	vkcu_range_push("vkhel_vector_polymul_lift");
-	const int st = polymul_impl(a, b, res, t, steps, nsteps);
+	const int st = polymul_impl(a, b, res, t, steps, nsteps, 0);
 	vkcu_range_pop();
 	return st;
 }
 
 static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector *b, struct vkhel_vector *res,
-		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps) {
+		struct vkhel_ntt_tables *t, const struct vkhel_lift_step *steps, uint32_t nsteps, int b_ntt) {
 	const struct vkh_devtab *d = NULL;
 	int st = check_transform("polymul", a, res, t, &d);
 	if (st)
 		return st;
 	if (!b || b->ctx != res->ctx || b->length < t->n)
 		return vkh_fail(res->ctx, VKHEL_ERR_INVALID_ARGUMENT, "polymul: bad operand b");
+	/* the composed path writes the result before it reads NTT(b) */
+	if (b_ntt && b->dev == res->dev)
+		return vkh_fail(res->ctx, VKHEL_ERR_INVALID_ARGUMENT, "polymul_ntt: result aliases NTT(b)");
 	struct vkhel_ctx *ctx = res->ctx;
 	vkcu_lift lift;
 	if ((st = vkh_lift_compile(ctx, steps, nsteps, t->q, &lift)))
@@ -646,26 +659,26 @@ static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector 
 			e = vkcu_lift_range(ctx->stream, res->dev, 1, t->q, lp);
 		return finish(ctx, e, "polymul");
 	}
-	uint64_t *scratch = res->dev;
+	uint64_t *scratch = b_ntt ? b->dev : res->dev;
 	void *tmp = NULL;
 	const int fused = t->log_n >= 8 && t->log_n <= vkcu_max_fused_log_n();
 	/* NTT(b) is parked in the result vector unless that would overwrite a
 	 * before it is read (the fused kernel reads a after writing NTT(b)), or
-	 * the transform needs its own output buffer. */
-	if (!fused || res->dev == a->dev) {
+	 * the transform needs its own output buffer; a given NTT(b) needs none. */
+	if (!b_ntt && (!fused || res->dev == a->dev)) {
 		if ((st = vkh_dev_alloc(ctx, bytes, &tmp)))
 			return st;
 		scratch = tmp;
 	}
 	int e;
 	if (fused) {
-		const vkcu_poly_job job = {a->dev, b->dev, res->dev, scratch, d->dev_set};
-		e = vkcu_polymul_lift(ctx->stream, NULL, 1, &job, t->log_n, vkcu_wide(t->q), ctx->sms, lp);
+		const vkcu_poly_job job = {a->dev, b->dev, res->dev, scratch, d->dev_set, b_ntt ? VKCU_JOB_B_NTT : 0};
+		e = vkcu_polymul_lift(ctx->stream, NULL, 1, &job, t->log_n, vkcu_wide(t->q), ctx->sms, lp, b_ntt);
 	} else {
 		const vkcu_ntt_job jb = {b->dev, scratch, d->dev_set};
 		const vkcu_ntt_job ja = {a->dev, res->dev, d->dev_set};
 		const vkcu_ntt_job jc = {res->dev, res->dev, d->dev_set};
-		e = vkcu_ntt_forward(ctx->stream, NULL, 1, &jb, t->log_n, vkcu_wide(t->q), ctx->sms);
+		e = b_ntt ? 0 : vkcu_ntt_forward(ctx->stream, NULL, 1, &jb, t->log_n, vkcu_wide(t->q), ctx->sms);
 		if (!e)
 			e = vkcu_ntt_forward(ctx->stream, NULL, 1, &ja, t->log_n, vkcu_wide(t->q), ctx->sms);
 		if (!e)

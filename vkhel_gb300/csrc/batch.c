@@ -26,6 +26,7 @@ struct job_rec {
 	uint32_t needs_scratch;
 	uint32_t lift;         /* index into the batch's lift table, 0 = none */
 	uint32_t wide;         /* modulus class: 2^62 <= q < 2^63 */
+	uint32_t b_ntt;        /* b holds NTT(b) (VKCU_JOB_B_NTT) */
 	uint32_t order;        /* insertion order, keeps the sort stable */
 	vkcu_poly_job job;
 };
@@ -99,10 +100,10 @@ static int lift_index(struct vkhel_batch *b, const vkcu_lift *l, uint32_t *idx) 
 	return VKHEL_OK;
 }
 
-/* Limb jobs of one call: a polymul (a, bb -> c) or a transform (a -> c, bb
- * unused). */
+/* Limb jobs of one call: a polymul (a, bb -> c; bb holding NTT(b) when
+ * b_ntt) or a transform (a -> c, bb unused). */
 static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
-		const uint64_t *a, const uint64_t *bb, uint64_t *c, const vkcu_lift *lift, uint32_t kind) {
+		const uint64_t *a, const uint64_t *bb, uint64_t *c, const vkcu_lift *lift, uint32_t kind, int b_ntt) {
 	struct vkhel_ctx *ctx = b->ctx;
 	if (b->committed)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch: already committed");
@@ -111,6 +112,9 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 	if (((uintptr_t) a | (uintptr_t) bb | (uintptr_t) c) & 31)
 		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: pointers must be 32-byte aligned");
 	const uint64_t n = tables[0] ? tables[0]->n : 0;
+	/* the composed path (n outside the fused range) writes c before it reads NTT(b) */
+	if (b_ntt && bb < c + (uint64_t) limbs * n && c < bb + (uint64_t) limbs * n)
+		return vkh_fail(ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: c overlaps NTT(b)");
 	for (uint32_t k = 0; k < limbs; k++) {
 		const struct vkhel_ntt_tables *t = tables[k];
 		if (!t || t->n != n || n < 2)
@@ -154,15 +158,18 @@ static int add_jobs(struct vkhel_batch *b, struct vkhel_ntt_tables *const *table
 		const int overlap = ak < ck + n && ck < ak + n;
 		r->kind = kind;
 		r->log_n = log_n;
-		r->needs_scratch = kind == VKH_JOB_POLYMUL && (!fused || overlap);
+		r->needs_scratch = kind == VKH_JOB_POLYMUL && !b_ntt && (!fused || overlap);
 		r->lift = lift_id;
 		r->wide = (uint32_t) vkcu_wide(tables[k]->q);
+		r->b_ntt = (uint32_t) (b_ntt != 0);
 		r->order = b->njobs - 1;
 		r->job.a = ak;
 		r->job.b = kind == VKH_JOB_POLYMUL ? bk : NULL;
 		r->job.c = ck;
-		r->job.scratch = ck;
+		/* NTT(b) given: the composed path's pointwise step reads it as the scratch */
+		r->job.scratch = b_ntt ? (uint64_t *) bk : ck;
 		r->job.tw = d->dev_set;
+		r->job.flags = b_ntt ? VKCU_JOB_B_NTT : 0;
 	}
 	return VKHEL_OK;
 }
@@ -178,7 +185,28 @@ int vkhel_batch_add_polymul(struct vkhel_batch *b, struct vkhel_ntt_tables *cons
 	const uint64_t need = (uint64_t) limbs * tables[0]->n;
 	if (a->length < need || bb->length < need || c->length < need)
 		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors shorter than limbs * n");
-	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, NULL, VKH_JOB_POLYMUL);
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, NULL, VKH_JOB_POLYMUL, 0);
+}
+
+int vkhel_batch_add_polymul_ntt(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const struct vkhel_vector *a, const struct vkhel_vector *b_ntt, struct vkhel_vector *c) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
+	if (!a || !b_ntt || !c || !tables || !tables[0])
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL argument");
+	if (a->ctx != b->ctx || b_ntt->ctx != b->ctx || c->ctx != b->ctx)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors of another context");
+	const uint64_t need = (uint64_t) limbs * tables[0]->n;
+	if (a->length < need || b_ntt->length < need || c->length < need)
+		return vkh_fail(b->ctx, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: vectors shorter than limbs * n");
+	return add_jobs(b, tables, limbs, a->dev, b_ntt->dev, c->dev, NULL, VKH_JOB_POLYMUL, 1);
+}
+
+int vkhel_batch_add_polymul_ntt_raw(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b_ntt, uint64_t *c) {
+	if (!b)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
+	return add_jobs(b, tables, limbs, a, b_ntt, c, NULL, VKH_JOB_POLYMUL, 1);
 }
 
 int vkhel_batch_add_polymul_lift(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
@@ -198,7 +226,7 @@ int vkhel_batch_add_polymul_lift(struct vkhel_batch *b, struct vkhel_ntt_tables 
 	const int st = vkh_lift_compile(b->ctx, steps, nsteps, 0, &lift);
 	if (st)
 		return st;
-	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, &lift, VKH_JOB_POLYMUL);
+	return add_jobs(b, tables, limbs, a->dev, bb->dev, c->dev, &lift, VKH_JOB_POLYMUL, 0);
 }
 
 int vkhel_batch_add_transform(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
@@ -222,14 +250,14 @@ int vkhel_batch_add_transform(struct vkhel_batch *b, struct vkhel_ntt_tables *co
 	if (st)
 		return st;
 	return add_jobs(b, tables, limbs, in->dev, NULL, out->dev, &lift,
-			direction == VKHEL_TRANSFORM_FORWARD ? VKH_JOB_FORWARD : VKH_JOB_INVERSE);
+			direction == VKHEL_TRANSFORM_FORWARD ? VKH_JOB_FORWARD : VKH_JOB_INVERSE, 0);
 }
 
 int vkhel_batch_add_polymul_raw(struct vkhel_batch *b, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
 		const uint64_t *a, const uint64_t *bb, uint64_t *c) {
 	if (!b)
 		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "batch_add: NULL batch");
-	return add_jobs(b, tables, limbs, a, bb, c, NULL, VKH_JOB_POLYMUL);
+	return add_jobs(b, tables, limbs, a, bb, c, NULL, VKH_JOB_POLYMUL, 0);
 }
 
 static int cmp_rec(const void *x, const void *y) {
@@ -242,6 +270,8 @@ static int cmp_rec(const void *x, const void *y) {
 		return (a->wide > b->wide) - (a->wide < b->wide);
 	if (a->lift != b->lift)
 		return (a->lift > b->lift) - (a->lift < b->lift);
+	if (a->b_ntt != b->b_ntt)
+		return (a->b_ntt > b->b_ntt) - (a->b_ntt < b->b_ntt);
 	return (a->order > b->order) - (a->order < b->order);
 }
 
@@ -263,10 +293,10 @@ int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, cons
 			e = vkcu_ntt_inverse_lift(stream, tj, (int) cl->count, NULL, cl->log_n, cl->wide, sms, lift);
 		} else if (cl->fused) {
 			e = vkcu_polymul_lift(stream, dev_poly + cl->first, (int) cl->count, NULL, cl->log_n, cl->wide, sms,
-					lift);
+					lift, (int) cl->b_ntt);
 		} else {
 			const vkcu_ntt_job *nj = dev_ntt + 3 * (size_t) cl->first;
-			e = vkcu_ntt_forward(stream, nj, (int) cl->count, NULL, cl->log_n, cl->wide, sms);
+			e = cl->b_ntt ? 0 : vkcu_ntt_forward(stream, nj, (int) cl->count, NULL, cl->log_n, cl->wide, sms);
 			if (!e)
 				e = vkcu_ntt_forward(stream, nj + cl->count, (int) cl->count, NULL, cl->log_n, cl->wide, sms);
 			if (!e)
@@ -361,8 +391,8 @@ static int ragged_setup(struct vkhel_batch *b) {
 	uint32_t first[17] = {0}, count[17] = {0};
 	for (uint32_t k = 0; k < b->nclasses; k++) {
 		const struct vkh_job_class *cl = &b->classes[k];
-		if (cl->kind != VKH_JOB_POLYMUL || !cl->fused || cl->wide || cl->lift || cl->log_n < 12 || cl->log_n > 16 ||
-				count[cl->log_n])
+		if (cl->kind != VKH_JOB_POLYMUL || !cl->fused || cl->wide || cl->lift || cl->b_ntt || cl->log_n < 12 ||
+				cl->log_n > 16 || count[cl->log_n])
 			return VKHEL_OK;
 		first[cl->log_n] = cl->first;
 		count[cl->log_n] = cl->count;
@@ -458,7 +488,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 		struct job_rec *r = &b->recs[i];
 		if (b->nclasses == 0 || b->classes[b->nclasses - 1].kind != r->kind ||
 				b->classes[b->nclasses - 1].log_n != r->log_n || b->classes[b->nclasses - 1].wide != (int) r->wide ||
-				b->classes[b->nclasses - 1].lift != r->lift) {
+				b->classes[b->nclasses - 1].lift != r->lift || b->classes[b->nclasses - 1].b_ntt != r->b_ntt) {
 			if (b->nclasses == MAX_CLASSES)
 				return vkh_fail(ctx, VKHEL_ERR_UNSUPPORTED, "batch_commit: too many degree classes");
 			struct vkh_job_class *cl = &b->classes[b->nclasses++];
@@ -466,6 +496,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 			cl->log_n = r->log_n;
 			cl->wide = (int) r->wide;
 			cl->lift = r->lift;
+			cl->b_ntt = r->b_ntt;
 			cl->first = i;
 			cl->count = 0;
 			cl->fused = r->log_n >= 8 && r->log_n <= vkcu_max_fused_log_n();

@@ -107,6 +107,7 @@ struct vkh_job_class {
 	int fused;
 	int wide;              /* modulus class of every job: 2^62 <= q < 2^63 */
 	uint32_t lift;         /* index into the lift table, 0 = none */
+	uint32_t b_ntt;        /* polymul jobs whose b holds NTT(b) (VKCU_JOB_B_NTT) */
 };
 /* lifts: table indexed by vkh_job_class.lift (NULL when no class has one) */
 int vkh_issue_classes(void *stream, int sms, const vkcu_poly_job *dev_poly, const vkcu_ntt_job *dev_ntt,

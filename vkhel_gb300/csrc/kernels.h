@@ -35,13 +35,18 @@ typedef struct vkcu_ntt_job {
 } vkcu_ntt_job;
 
 /* One negacyclic limb product c = a * b mod (X^n + 1, q).  `scratch` holds n
- * words for NTT(b) during the kernel; it may be `c` unless c overlaps a. */
+ * words for NTT(b) during the kernel; it may be `c` unless c overlaps a.
+ * With VKCU_JOB_B_NTT in `flags`, b already holds NTT(b) (bit-reversed, as
+ * the forward transform writes it; words reduced as elemmul reduces its
+ * operands) and `scratch` is unused: c = INTT(NTT(a) . b). */
+#define VKCU_JOB_B_NTT 1u
 typedef struct vkcu_poly_job {
 	const uint64_t *a;
 	const uint64_t *b;
 	uint64_t *c;
 	uint64_t *scratch;
 	const vkcu_twset *tw;        /* device pointer */
+	uint64_t flags;              /* VKCU_JOB_* */
 } vkcu_poly_job;
 
 /* ---- runtime (runtime.cu) ---- */
@@ -161,11 +166,14 @@ int vkcu_ntt_inverse(void *stream, const vkcu_ntt_job *jobs, int njobs,
 int vkcu_polymul(void *stream, const vkcu_poly_job *jobs, int njobs,
 		const vkcu_poly_job *one, uint32_t log_n, int wide, int sms);
 /* The same with an epilogue (`lift` NULL or count 0: none); fused into the
- * last pass for 2^8 <= n <= 2^17, a separate element-wise launch otherwise. */
+ * last pass for 2^8 <= n <= 2^17, a separate element-wise launch otherwise.
+ * b_ntt: the jobs carry VKCU_JOB_B_NTT; only the epilogue instantiations of
+ * the fused kernels read that flag, so such jobs run those (with no steps
+ * when `lift` has none) and the plain kernels stay as lean as before. */
 int vkcu_ntt_inverse_lift(void *stream, const vkcu_ntt_job *jobs, int njobs,
 		const vkcu_ntt_job *one, uint32_t log_n, int wide, int sms, const vkcu_lift *lift);
 int vkcu_polymul_lift(void *stream, const vkcu_poly_job *jobs, int njobs,
-		const vkcu_poly_job *one, uint32_t log_n, int wide, int sms, const vkcu_lift *lift);
+		const vkcu_poly_job *one, uint32_t log_n, int wide, int sms, const vkcu_lift *lift, int b_ntt);
 /* The epilogue alone, in place on `len` words at p (modulus q for TABLE_Q
  * steps), or on the n output words of every job. */
 int vkcu_lift_range(void *stream, uint64_t *p, uint64_t len, uint64_t q, const vkcu_lift *lift);

@@ -321,19 +321,20 @@ extern "C" int vkcu_ntt_inverse(void* stream, const vkcu_ntt_job* jobs, int njob
 }
 
 extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,
-                                 uint32_t log_n, int wide, int sms, const vkcu_lift* lift) {
+                                 uint32_t log_n, int wide, int sms, const vkcu_lift* lift, int b_ntt) {
   cudaStream_t st = (cudaStream_t)stream;
   const vkcu_poly_job o = one ? *one : vkcu_poly_job{};
   if (log_n < 8 || log_n > (uint32_t)kMaxCluster || njobs < 1) return (int)cudaErrorInvalidValue;
   if (has_lift(lift) && lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
-  const vkcu_lift* lp = has_lift(lift) ? lift : nullptr;
+  static const vkcu_lift kNoSteps{};  // the epilogue instantiations with nothing to apply
+  const vkcu_lift* lp = has_lift(lift) ? lift : b_ntt ? &kNoSteps : nullptr;
   if (wide) {
     if (log_n <= (uint32_t)kMaxCta) return poly_cta_wide(st, jobs, njobs, o, (int)log_n, sms, lp);
     return poly_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta, lp);
   }
   if (split_small(njobs, log_n, sms)) return poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
   if (log_n <= (uint32_t)kMaxCta) {
-    if (lp) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms), *lift);
+    if (lp) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms), *lp);
     return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms));
   }
   return poly_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta, lp);
@@ -341,7 +342,7 @@ extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int nj
 
 extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, const vkcu_poly_job* one,
                             uint32_t log_n, int wide, int sms) {
-  return vkcu_polymul_lift(stream, jobs, njobs, one, log_n, wide, sms, nullptr);
+  return vkcu_polymul_lift(stream, jobs, njobs, one, log_n, wide, sms, nullptr, 0);
 }
 
 // The epilogue as its own element-wise pass: over `len` words at p, or over
@@ -394,8 +395,9 @@ extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs,
 }
 
 // Pointwise step of a composed polymul: c = c * scratch mod q over njobs
-// jobs of n words each (both operands canonical NTT outputs), the word the
-// reference's elemmul stores.
+// jobs of n words each, the word the reference's elemmul stores: c is a
+// canonical NTT output, scratch one too or the caller's NTT(b), reduced as
+// elemmul reduces its operands.
 template <class M>
 __global__ void k_pointwise(const vkcu_poly_job* __restrict__ jobs, int njobs, int log_n) {
   const long n = 1L << log_n;
@@ -405,7 +407,7 @@ __global__ void k_pointwise(const vkcu_poly_job* __restrict__ jobs, int njobs, i
     const long i = w & (n - 1);
     const Tw t = load_tw(job.tw);
     u64* c = reinterpret_cast<u64*>(job.c);
-    const u64 x = c[i], y = reinterpret_cast<const u64*>(job.scratch)[i];
+    const u64 x = c[i], y = ref_reduce64_maybe(reinterpret_cast<const u64*>(job.scratch)[i], t.q, t.mu, t.qbits);
     c[i] = M::product_out(x, y, t);
   }
 }

@@ -208,11 +208,14 @@ __global__ void __launch_bounds__(S::T, 1)
   for (int w = cid; w < njobs; w += ncl) {
     const vkcu_poly_job job = fetch_job(jobs, one, w);
     const Tw t = load_tw(job.tw);
-    u64* scratch = reinterpret_cast<u64*>(job.scratch) + (size_t)rank * K::SUB;
+    // b holds NTT(b): phase 0 is skipped (read by the epilogue instantiations only)
+    const bool b_ntt = LIFT && (job.flags & VKCU_JOB_B_NTT);
+    u64* scratch = (b_ntt ? const_cast<u64*>(reinterpret_cast<const u64*>(job.b)) : reinterpret_cast<u64*>(job.scratch)) +
+                   (size_t)rank * K::SUB;
     if ((int)threadIdx.x < K::C)  // this CTA's column slices of a, for phase 1
       prefetch_l2(reinterpret_cast<const u64*>(job.a) + (size_t)threadIdx.x * K::SUB + rank * K::COLS, kSlice);
 #pragma unroll 1
-    for (int ph = 0; ph < 2; ph++) {
+    for (int ph = b_ntt ? 1 : 0; ph < 2; ph++) {
       cluster_arrive();  // done with every shared memory the column pass writes (col_fwd waits)
       col_fwd<LOGC, S, true>(reinterpret_cast<const u64*>(ph ? job.a : job.b), sm, cl, rank, t);
       cl.sync();
@@ -226,6 +229,7 @@ __global__ void __launch_bounds__(S::T, 1)
         } else {
           u64 bh[16];
           load16(bh, scratch + 16 * g);
+          if (b_ntt) reduce_operand16(bh, t);
 #pragma unroll
           for (int j = 0; j < 16; j++) v[j] = M::product(v[j], bh[j], t);
           // the sub-block's first inverse pass (stages HEAD + 3 .. HEAD) on the same words
@@ -236,8 +240,11 @@ __global__ void __launch_bounds__(S::T, 1)
       });
     }
     if (w + ncl < njobs && (int)threadIdx.x < K::C) {
+      // the next job's b: its column slices, or (NTT(b) given) this CTA's sub-block
       const vkcu_poly_job nx = fetch_job(jobs, one, w + ncl);
-      prefetch_l2(reinterpret_cast<const u64*>(nx.b) + (size_t)threadIdx.x * K::SUB + rank * K::COLS, kSlice);
+      const size_t off = (LIFT && (nx.flags & VKCU_JOB_B_NTT)) ? (size_t)rank * K::SUB + (size_t)threadIdx.x * K::COLS
+                                                     : (size_t)threadIdx.x * K::SUB + rank * K::COLS;
+      prefetch_l2(reinterpret_cast<const u64*>(nx.b) + off, kSlice);
     }
     inv_passes<S>(sm, t, tw_mult, S::HEAD - 4);
     inv_last_smem<S>(sm, t, tw_mult);

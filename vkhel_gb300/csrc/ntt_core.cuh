@@ -106,6 +106,13 @@ __device__ __forceinline__ Tw load_tw(const vkcu_twset* p) {
   return t;
 }
 
+// A caller-supplied NTT(b) operand reduced as the reference's elemmul reduces
+// its operands (reduce64, elemmul.comp:36-47): canonical words pass through.
+__device__ __forceinline__ void reduce_operand16(u64 (&v)[16], const Tw& t) {
+#pragma unroll
+  for (int j = 0; j < 16; j++) v[j] = ref_reduce64_maybe(v[j], t.q, t.mu, t.qbits);
+}
+
 // ---------------------------------------------------------------------------
 // First-stage butterflies with the reference's exact semantics.
 
@@ -689,10 +696,12 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E, true>())
   for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
     const vkcu_poly_job job = fetch_job(jobs, one, w);
     const Tw t = load_tw(job.tw);
-    u64* scratch = reinterpret_cast<u64*>(job.scratch);
+    // b holds NTT(b): phase 0 is skipped (read by the epilogue instantiations only)
+    const bool b_ntt = LIFT && (job.flags & VKCU_JOB_B_NTT);
+    u64* scratch = b_ntt ? const_cast<u64*>(reinterpret_cast<const u64*>(job.b)) : reinterpret_cast<u64*>(job.scratch);
     if (threadIdx.x < 4) prefetch_l2(reinterpret_cast<const char*>(job.a) + threadIdx.x * kChunk, kChunk);
 #pragma unroll 1
-    for (int ph = 0; ph < 2; ph++) {
+    for (int ph = b_ntt ? 1 : 0; ph < 2; ph++) {
       fwd_first<S>(sm, reinterpret_cast<const u64*>(ph ? job.a : job.b), t, 1u);
       if (ph == 1 && w + (int)gridDim.x < njobs && threadIdx.x < 4) {
         const vkcu_poly_job nx = fetch_job(jobs, one, w + (int)gridDim.x);
@@ -706,6 +715,7 @@ __global__ void __launch_bounds__((1 << LOGN) / E, min_blocks<LOGN, E, true>())
         } else {
           u64 bh[16];
           load16(bh, scratch + 16 * g);
+          if (b_ntt) reduce_operand16(bh, t);
 #pragma unroll
           for (int j = 0; j < 16; j++) v[j] = M::product(v[j], bh[j], t);
           // the first inverse pass (stages HEAD + 3 .. HEAD) on the same 16 words

@@ -186,6 +186,7 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 			cl->log_n = log_n;
 			cl->wide = wide;
 			cl->lift = 0;
+			cl->b_ntt = 0;
 			cl->first = i;
 			cl->count = 0;
 			cl->fused = fused_log_n(log_n);
@@ -252,7 +253,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 			if (e)
 				break;
 			uint64_t *base = r->dev;
-			vkcu_poly_job j;
+			vkcu_poly_job j = {0};
 			j.a = base + (uint64_t) k * r->n;
 			j.b = base + words + (uint64_t) k * r->n;
 			j.c = base + 2 * words + (uint64_t) k * r->n;
