@@ -25,6 +25,8 @@ the device so that a profiler capture of one launch ends quickly.
                 the words past n of an inverse transform      k_elementwise<...>, k_lift_range
   wide_transforms  1024 forward transforms of n = 2^14 and 64 of n = 2^16, 63-bit primes
                 k_ntt_fwd<14,..,Mod63>, k_ntt_fwd_cluster<2, Shape<14,32,1,Mod63>>
+  ntt_operand   256 polymuls of n = 2^14 with b given as NTT(b)  k_polymul<14,..,true> (the
+                epilogue instantiation, no steps)
 """
 import argparse
 import sys
@@ -121,6 +123,24 @@ def case_wide_polymul(ctx):
 
 def case_cluster_polymul(ctx):
     return _polymul_batch(ctx, 1 << 16, 64, primes=1)
+
+
+def case_ntt_operand(ctx):
+    n, jobs, primes = 1 << 14, 256, 8
+    qs, tabs = _tabs(n, primes)
+    a, b = _operands(ctx, n, qs, jobs, 1), _operands(ctx, n, qs, jobs, 2)
+    bn, c = vk.Vector(ctx, jobs * n), vk.Vector(ctx, jobs * n)
+    ft = vk.Batch(ctx)  # NTT(b), once, outside the profiled launches
+    ft.add_transform([tabs[j % primes] for j in range(jobs)], b, bn)
+    ft.commit(graph=False)
+    ft.run()
+    ft.close()
+    bt = vk.Batch(ctx)
+    for j in range(0, jobs, primes):
+        bt.add_polymul(tabs, a.device_ptr + 8 * j * n, bn.device_ptr + 8 * j * n, c.device_ptr + 8 * j * n,
+                       b_ntt=True)
+    bt.commit(graph=True)
+    return bt.launch, (bt, a, b, bn, c, tabs)
 
 
 def case_ragged_single(ctx):
