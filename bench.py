@@ -267,7 +267,8 @@ def serving_sweep(vk, torch, orc, rates=(1000, 4000, 16000, None), seconds=1.0, 
         for _ in range(2):  # and the device pool grown to what many requests in flight hold
             for r in [srv.submit(p_[2], p_[3], p_[4], p_[5]) for p_ in pay]:
                 srv.wait(r)
-        for rate in rates:
+        def drive(rate, submit):
+            """Poisson arrivals at `rate` (None: all at once) of the payloads in turn."""
             count = int(min(6000, (rate or 20000) * seconds)) if rate else 2000
             gaps = rng.exponential(1.0 / rate, size=count) if rate else np.zeros(count)
             srv.reset_stats()
@@ -283,24 +284,38 @@ def serving_sweep(vk, torch, orc, rates=(1000, 4000, 16000, None), seconds=1.0, 
                         break
                     if lag > 2e-4:
                         time.sleep(lag - 1e-4)
-                p_ = pay[i % payloads]
-                ids.append(srv.submit(p_[2], p_[3], p_[4], p_[5]))
-                limbs += p_[1]
+                ids.append(submit(i % payloads))
+                limbs += pay[i % payloads][1]
             fails = sum(srv.wait(r) != 0 for r in ids)
             st = srv.stats()
-            out["rates"].append({
-                "offered_req_per_s": rate if rate else "saturation", "requests": count,
-                "achieved_req_per_s": st["completed"] / st["span_s"] if st["span_s"] else None,
-                "limb_polymul_per_s": limbs / st["span_s"] if st["span_s"] else None,
-                "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
-                "micro_batches": st["batches"], "failed": fails})
+            return {"offered_req_per_s": rate if rate else "saturation", "requests": count,
+                    "achieved_req_per_s": st["completed"] / st["span_s"] if st["span_s"] else None,
+                    "limb_polymul_per_s": limbs / st["span_s"] if st["span_s"] else None,
+                    "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                    "micro_batches": st["batches"], "failed": fails}
+
+        plain = lambda i: srv.submit(pay[i][2], pay[i][3], pay[i][4], pay[i][5])
+        for rate in rates:
+            out["rates"].append(drive(rate, plain))
+        # resident operands: every payload's b uploaded once (transformed on
+        # the device) and kept; its requests bring a only
+        oids = [srv.add_operand(p_[2], p_[4]) for p_ in pay]
+        resident = lambda i: srv.submit_operand(pay[i][2], pay[i][3], oids[i], pay[i][5])
+        for r in [resident(i) for i in range(payloads)]:  # warm-up
+            srv.wait(r)
+        out["resident_operands"] = {
+            "workload": "the same payloads, each b kept on the server as a resident operand "
+                        "(vkhel_server_add_operand, transformed on the device once); requests upload a only",
+            "rates": [drive(rate, resident) for rate in (1000, 4000, None)]}
+        for o in oids:
+            srv.remove_operand(o)
     # every payload's result (its last run) against the oracle, all limbs
     for n, limbs, tl, a, b, c, qs, ws in pay:
         an, bn, cn = (x.numpy().view(np.uint64).reshape(-1, n) for x in (a, b, c))
         ref, _ = orc.polymul_batch(an, bn, n, qs, ws, np.arange(limbs, dtype=np.uint32),
                                    tables=orc.batch_tables(n, qs, ws))
         assert np.array_equal(cn, ref), "serving result differs from the oracle"
-    out["checked_against_oracle"] = f"all {payloads} payloads, every limb"
+    out["checked_against_oracle"] = f"all {payloads} payloads, every limb (their last run: with resident operands)"
     # plain per-call path: upload, forward x2, elemmul, inverse, download per limb
     ctx = vk.Context()
     lat = []

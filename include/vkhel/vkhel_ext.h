@@ -313,6 +313,24 @@ int vkhel_server_cancel(struct vkhel_server *s, int64_t id);
  * VKHEL_ERR_TIMEOUT (the request stays pending and can be waited for again).
  * After a non-timeout return the id is collected and cannot be waited again. */
 int vkhel_server_wait(struct vkhel_server *s, int64_t id, uint32_t timeout_ms);
+/* Resident operands: `limbs` limb polynomials that many requests multiply by
+ * (a key, a plaintext), uploaded once and kept on the server's device in the
+ * transform domain.  b holds b (is_ntt 0: transformed on the device) or
+ * NTT(b) as vkhel_vector_forward_transform writes it (is_ntt 1), limb-major;
+ * it is read before the call returns.  Returns an operand id > 0, or
+ * -status.  The upload runs in queue order on the scheduler. */
+int64_t vkhel_server_add_operand(struct vkhel_server *s,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *b, int is_ntt);
+/* A request c = a * b with b the resident operand `operand`, whose limbs must
+ * have these tables' (n, q, w): only a is uploaded.  Returns a request id,
+ * or -status; wait for it as for vkhel_server_submit. */
+int64_t vkhel_server_submit_operand(struct vkhel_server *s,
+		struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, int64_t operand, uint64_t *c);
+/* Frees a resident operand; INVALID_ARGUMENT while queued or running
+ * requests still read it (wait for them first) or for an unknown id. */
+int vkhel_server_remove_operand(struct vkhel_server *s, int64_t operand);
 int vkhel_server_stats(struct vkhel_server *s, struct vkhel_server_stats *out);
 int vkhel_server_reset_stats(struct vkhel_server *s);
 /* Runs the remaining queue to completion, then frees everything. */

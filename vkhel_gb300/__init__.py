@@ -104,6 +104,9 @@ _SIGNATURES = [
     ("vkhel_tune_load", ctypes.c_int, [ctypes.c_char_p]),
     ("vkhel_server_create", vp, [vp]),
     ("vkhel_server_submit", ctypes.c_int64, [vp, ctypes.POINTER(vp), u32, vp, vp, vp]),
+    ("vkhel_server_add_operand", ctypes.c_int64, [vp, ctypes.POINTER(vp), u32, vp, ctypes.c_int]),
+    ("vkhel_server_submit_operand", ctypes.c_int64, [vp, ctypes.POINTER(vp), u32, vp, ctypes.c_int64, vp]),
+    ("vkhel_server_remove_operand", ctypes.c_int, [vp, ctypes.c_int64]),
     ("vkhel_server_wait", ctypes.c_int, [vp, ctypes.c_int64, u32]),
     ("vkhel_server_stats", ctypes.c_int, [vp, vp]),
     ("vkhel_server_reset_stats", ctypes.c_int, [vp]),
@@ -594,6 +597,7 @@ class Server:
             code, msg = last_error(None)
             raise VkhelError(code or 4, msg)
         self._pending = {}
+        self._operands = {}
 
     def submit(self, tables, a, b, c):
         arr = (vp * len(tables))(*[t.ptr for t in tables])
@@ -604,6 +608,36 @@ class Server:
             raise VkhelError(-rid, msg)
         self._pending[rid] = (tables, a, b, c)
         return rid
+
+    def add_operand(self, tables, b, is_ntt=False):
+        """Keep b (or NTT(b), is_ntt=True) resident on the server; returns the operand id."""
+        arr = (vp * len(tables))(*[t.ptr for t in tables])
+        oid = lib().vkhel_server_add_operand(self.ptr, arr, len(tables), _ptr(b), 1 if is_ntt else 0)
+        if oid < 0:
+            code, msg = last_error(None)
+            lib().vkhel_ctx_clear_error(None)
+            raise VkhelError(-oid, msg)
+        self._operands[oid] = tables
+        return oid
+
+    def submit_operand(self, tables, a, operand, c):
+        """A request c = a * b with b the resident operand `operand`."""
+        arr = (vp * len(tables))(*[t.ptr for t in tables])
+        rid = lib().vkhel_server_submit_operand(self.ptr, arr, len(tables), _ptr(a), int(operand), _ptr(c))
+        if rid < 0:
+            code, msg = last_error(None)
+            lib().vkhel_ctx_clear_error(None)
+            raise VkhelError(-rid, msg)
+        self._pending[rid] = (tables, a, c)
+        return rid
+
+    def remove_operand(self, operand):
+        st = lib().vkhel_server_remove_operand(self.ptr, int(operand))
+        if st:
+            code, msg = last_error(None)
+            lib().vkhel_ctx_clear_error(None)
+            raise VkhelError(st, msg)
+        self._operands.pop(operand, None)
 
     def cancel(self, rid):
         """Cancel a request still queued; returns its status code (0 = cancelled)."""

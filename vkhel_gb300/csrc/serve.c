@@ -22,6 +22,11 @@
  *     requests, releases their memory and wakes waiters and the scheduler
  *     (slower event polls catch a failed stream); requests that arrive while
  *     others run join the next micro-batch.
+ * Resident operands: a polynomial that many requests multiply by (a key, a
+ * plaintext) can be uploaded once and kept in the transform domain; its
+ * requests then upload only a, and their products skip NTT(b).  The upload
+ * runs on the scheduler thread, in queue order (all use of the server's
+ * context stays on that thread).
  * Every limb product is computed exactly as in the plain API, so a request's
  * result is the same alone and in any mix.  Latency = completion - submission
  * (monotonic clock), recorded per request.  All device work happens on the
@@ -35,9 +40,10 @@
 
 #include "internal.h"
 
-/* classes of one micro-batch: one per (degree, modulus class) present; the
- * first SRV_AUX + 1 of them can run on concurrent streams */
-#define SRV_MAX_CLASSES 64
+/* classes of one micro-batch: one per (degree, modulus class, resident
+ * operand or not) present, at most 4 per degree 2^1 .. 2^26; the first
+ * SRV_AUX + 1 of them can run on concurrent streams */
+#define SRV_MAX_CLASSES 104
 #define SRV_AUX 32
 /* At low load (the micro-batch took every queued request) a micro-batch of
  * at most SRV_CHUNKS requests and at least 2 SRV_CHUNK_MIN bytes of operands
@@ -51,6 +57,19 @@
 #define SRV_CHUNKS 4
 #define SRV_CHUNK_MIN ((uint64_t) 4 << 20)
 
+/* A resident operand: `limbs` limb polynomials kept on the device in the
+ * transform domain for the requests that multiply by them. */
+struct srv_operand {
+	uint32_t limbs, log_n;
+	uint64_t n;
+	struct vkhel_ntt_tables **tables; /* per limb; a request's (n, q, w) must match */
+	const uint64_t *host;             /* b or NTT(b), read by the upload */
+	int is_ntt;
+	void *dev;                        /* NTT(b), limbs * n words */
+	uint64_t bytes;
+	uint32_t users;                   /* queued and running requests that read it */
+};
+
 struct srv_req {
 	struct srv_req *next;
 	int64_t id;
@@ -59,6 +78,8 @@ struct srv_req {
 	const uint64_t *a, *b;
 	uint64_t *c;
 	struct vkhel_ntt_tables **tables;
+	struct srv_operand *op; /* b is this resident operand (b unused) */
+	int upload;             /* a queue entry that uploads `op` (no product) */
 	int state; /* 0 queued, 1 running, 2 finished */
 	int status;
 	double t_submit, t_done;
@@ -100,6 +121,8 @@ struct vkhel_server {
 	struct srv_req *q_head, *q_tail;
 	struct srv_req **by_id; /* index id - 1 */
 	int64_t next_id, cap_id;
+	struct srv_operand **ops; /* resident operands, index id - 1 (NULL: removed) */
+	int64_t nops, cap_ops;
 	double *lat_ms;
 	uint64_t nlat, cap_lat;
 	uint64_t submitted, completed, failed, batches, limbs_done;
@@ -116,10 +139,15 @@ static int fused_log_n(uint32_t log_n) {
 	return log_n >= 8 && log_n <= vkcu_max_fused_log_n();
 }
 
+/* Device words of a request: a, b, c (+ an NTT(b) scratch off the fused
+ * range); a and c only with a resident operand. */
 static uint64_t req_bytes(const struct srv_req *r) {
 	const uint64_t words = (uint64_t) r->limbs * r->n;
-	return 8 * words * (fused_log_n(r->log_n) ? 3 : 4);
+	return 8 * words * (r->op ? 2 : fused_log_n(r->log_n) ? 3 : 4);
 }
+
+/* Host bytes a request uploads per limb word: a and b, or a alone. */
+static uint64_t up_per_word(const struct srv_req *r) { return r->op ? 8 : 16; }
 
 static int cmp_job_log_n(const void *x, const void *y) {
 	const uint64_t a = *(const uint64_t *) x, b = *(const uint64_t *) y;
@@ -155,7 +183,7 @@ struct srv_seg {
 static uint32_t chunk_count(const struct vkhel_server *s, const struct srv_slot *sl, uint64_t *up_bytes) {
 	uint64_t b = 0;
 	for (uint32_t i = 0; i < sl->nreqs; i++)
-		b += 16 * (uint64_t) sl->reqs[i]->limbs * sl->reqs[i]->n;
+		b += up_per_word(sl->reqs[i]) * sl->reqs[i]->limbs * sl->reqs[i]->n;
 	*up_bytes = b;
 	if (!sl->chunkable || sl->nreqs > SRV_CHUNKS || b < 2 * SRV_CHUNK_MIN)
 		return 1;
@@ -176,9 +204,10 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 	for (uint32_t i = j0; i < j1; i++) {
 		const uint32_t log_n = (uint32_t) (keys[i] >> 40);
 		const int wide = (int) ((keys[i] >> 39) & 1);
-		sl->host_poly[i] = tmp[keys[i] & 0x7fffffffffull];
-		if (nclasses == 0 || classes[nclasses - 1].log_n != log_n || classes[nclasses - 1].wide != wide) {
-			/* at most two classes per degree 2^1 .. 2^26: 52 */
+		const uint32_t b_ntt = (uint32_t) ((keys[i] >> 38) & 1);
+		sl->host_poly[i] = tmp[keys[i] & 0x3fffffffffull];
+		if (nclasses == 0 || classes[nclasses - 1].log_n != log_n || classes[nclasses - 1].wide != wide ||
+				classes[nclasses - 1].b_ntt != b_ntt) {
 			if (nclasses == SRV_MAX_CLASSES)
 				return VKHEL_ERR_UNSUPPORTED;
 			struct vkh_job_class *cl = &classes[nclasses++];
@@ -186,7 +215,7 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 			cl->log_n = log_n;
 			cl->wide = wide;
 			cl->lift = 0;
-			cl->b_ntt = 0;
+			cl->b_ntt = b_ntt;
 			cl->first = i;
 			cl->count = 0;
 			cl->fused = fused_log_n(log_n);
@@ -216,7 +245,7 @@ static int issue_chunk(struct vkhel_server *s, struct srv_slot *sl, uint32_t c, 
 	for (uint32_t g = 0; !e && g < nsegs; g++) {
 		struct srv_req *r = sl->reqs[segs[g].req];
 		const uint64_t words = (uint64_t) r->limbs * r->n, off = (uint64_t) segs[g].k0 * r->n;
-		e = vkcu_d2h(s->s_out, r->c + off, (uint64_t *) r->dev + 2 * words + off,
+		e = vkcu_d2h(s->s_out, r->c + off, (uint64_t *) r->dev + (r->op ? 1 : 2) * words + off,
 				8 * (size_t) (segs[g].k1 - segs[g].k0) * r->n);
 	}
 	return e;
@@ -255,13 +284,21 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 			uint64_t *base = r->dev;
 			vkcu_poly_job j = {0};
 			j.a = base + (uint64_t) k * r->n;
-			j.b = base + words + (uint64_t) k * r->n;
-			j.c = base + 2 * words + (uint64_t) k * r->n;
-			j.scratch = fused ? j.c : base + 3 * words + (uint64_t) k * r->n;
+			if (r->op) { /* device layout a, c; b is the resident NTT(b) */
+				j.b = (const uint64_t *) r->op->dev + (uint64_t) k * r->n;
+				j.c = base + words + (uint64_t) k * r->n;
+				j.scratch = (uint64_t *) j.b; /* read by the composed path's pointwise step */
+				j.flags = VKCU_JOB_B_NTT;
+			} else { /* a, b, c (+ scratch) */
+				j.b = base + words + (uint64_t) k * r->n;
+				j.c = base + 2 * words + (uint64_t) k * r->n;
+				j.scratch = fused ? j.c : base + 3 * words + (uint64_t) k * r->n;
+			}
 			j.tw = d->dev_set;
-			keys[njobs] = ((uint64_t) r->log_n << 40) | ((uint64_t) vkcu_wide(r->tables[k]->q) << 39) | njobs;
+			keys[njobs] = ((uint64_t) r->log_n << 40) | ((uint64_t) vkcu_wide(r->tables[k]->q) << 39) |
+					((uint64_t) (r->op != NULL) << 38) | njobs;
 			tmp[njobs++] = j;
-			acc += 16 * r->n;
+			acc += up_per_word(r) * r->n;
 			const int last = i + 1 == sl->nreqs && k + 1 == r->limbs;
 			const int close = last || (c + 1 < nchunks && acc * nchunks >= up_bytes * (c + 1));
 			if (close || k + 1 == r->limbs) { /* a segment ends: upload it */
@@ -271,7 +308,7 @@ static void launch_slot(struct vkhel_server *s, struct srv_slot *sl) {
 				k0 = k + 1;
 				issued = 1;
 				e = vkcu_h2d(s->s_in, (uint64_t *) r->dev + off, r->a + off, len);
-				if (!e)
+				if (!e && !r->op)
 					e = vkcu_h2d(s->s_in, (uint64_t *) r->dev + words + off, r->b + off, len);
 			}
 			if (!e && close) {
@@ -323,6 +360,8 @@ static void finish_slot(struct vkhel_server *s, struct srv_slot *sl, int status)
 		r->state = 2;
 		r->t_done = t;
 		s->bytes -= r->dev_bytes;
+		if (r->op)
+			r->op->users--;
 		if (r->status == 0) {
 			s->completed++;
 			s->limbs_done += r->limbs;
@@ -340,6 +379,39 @@ static void finish_slot(struct vkhel_server *s, struct srv_slot *sl, int status)
 	sl->busy = 0;
 	s->batches++;
 	pthread_cond_broadcast(&s->cv_done);
+}
+
+/* Upload a resident operand (scheduler thread, no lock): b or NTT(b) into a
+ * pool buffer on the input stream, then, for b, a forward transform of every
+ * limb in place; returns a status. */
+static int upload_operand(struct vkhel_server *s, struct srv_operand *op) {
+	struct vkhel_ctx *ctx = s->ctx;
+	op->bytes = 8 * (uint64_t) op->limbs * op->n;
+	if (vkh_inject_alloc_failure() || vkcu_alloc(ctx->pool, s->s_in, op->bytes, &op->dev)) {
+		op->dev = NULL;
+		return VKHEL_ERR_OUT_OF_MEMORY;
+	}
+	int st = VKHEL_OK;
+	int e = vkcu_h2d(s->s_in, op->dev, op->host, op->bytes);
+	for (uint32_t k = 0; !e && !st && !op->is_ntt && k < op->limbs; k++) {
+		const struct vkh_devtab *d = NULL;
+		st = vkh_devtab_get(ctx, op->tables[k], &d);
+		if (st)
+			break;
+		uint64_t *p = (uint64_t *) op->dev + (uint64_t) k * op->n;
+		const vkcu_ntt_job j = {p, p, d->dev_set};
+		e = vkcu_ntt_forward(s->s_in, NULL, 1, &j, op->log_n, vkcu_wide(op->tables[k]->q), ctx->sms);
+	}
+	const int se = vkcu_sync(s->s_in);
+	if (!e)
+		e = se;
+	if (!st && e)
+		st = VKHEL_ERR_DEVICE;
+	if (st) {
+		vkcu_free(s->s_in, op->dev);
+		op->dev = NULL;
+	}
+	return st;
 }
 
 static void *scheduler(void *arg) {
@@ -381,10 +453,30 @@ static void *scheduler(void *arg) {
 			pthread_mutex_unlock(&s->mu);
 			break;
 		}
+		/* an operand upload at the head of the queue runs before anything
+		 * queued after it (requests that read it come later) */
+		if (s->q_head && s->q_head->upload) {
+			struct srv_req *r = s->q_head;
+			s->q_head = r->next;
+			if (!s->q_head)
+				s->q_tail = NULL;
+			r->state = 1;
+			pthread_mutex_unlock(&s->mu);
+			const int st = upload_operand(s, r->op);
+			pthread_mutex_lock(&s->mu);
+			r->status = st;
+			r->state = 2;
+			r->t_done = now_s();
+			pthread_cond_broadcast(&s->cv_done);
+			pthread_mutex_unlock(&s->mu);
+			continue;
+		}
 		uint32_t limbs = 0;
 		if (free_slot) {
 			while (s->q_head) {
 				struct srv_req *r = s->q_head;
+				if (r->upload) /* runs once this micro-batch is launched */
+					break;
 				if (free_slot->nreqs > 0 && limbs + r->limbs > s->max_limbs)
 					break;
 				if (s->budget && s->bytes + r->dev_bytes > s->budget && (inflight > 0 || free_slot->nreqs > 0))
@@ -507,60 +599,87 @@ struct vkhel_server *vkhel_server_create(const struct vkhel_server_config *cfg) 
 	return s;
 }
 
-int64_t vkhel_server_submit(struct vkhel_server *s, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
-		const uint64_t *a, const uint64_t *b, uint64_t *c) {
-	if (!s || !tables || !limbs || !a || !b || !c || !tables[0])
-		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit: bad arguments");
-	if (limbs > s->max_limbs)
-		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT,
-				"server_submit: %u limbs exceed the micro-batch size %u", limbs, s->max_limbs);
+/* The tables of one submission: every limb of one degree n >= 2 and a
+ * modulus the kernels take. */
+static int check_tables(struct vkhel_ntt_tables *const *tables, uint32_t limbs, const char *fn) {
 	const uint64_t n = tables[0]->n;
 	for (uint32_t k = 0; k < limbs; k++) {
 		const struct vkhel_ntt_tables *t = tables[k];
 		if (!t || t->n != n || n < 2)
-			return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit: limb %u tables invalid", k);
+			return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: limb %u tables invalid", fn, k);
 		if (t->q >= ((uint64_t) 1 << 63) || t->q < 3 || t->unreduced || t->log_n > vkcu_max_log_n())
-			return -vkh_fail(NULL, VKHEL_ERR_UNSUPPORTED, "server_submit: limb %u (n, q) unsupported", k);
+			return vkh_fail(NULL, VKHEL_ERR_UNSUPPORTED, "%s: limb %u (n, q) unsupported", fn, k);
 	}
+	return VKHEL_OK;
+}
+
+/* A request (or operand upload) for the given limbs, tables copied. */
+static struct srv_req *new_req(struct vkhel_ntt_tables *const *tables, uint32_t limbs) {
 	struct srv_req *r = calloc(1, sizeof(*r));
 	struct vkhel_ntt_tables **tcopy = malloc(sizeof(*tcopy) * limbs);
 	if (!r || !tcopy) {
 		free(r);
 		free(tcopy);
-		return -vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "server_submit: host allocation failed");
+		vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "server: host allocation failed");
+		return NULL;
 	}
 	memcpy(tcopy, tables, sizeof(*tcopy) * limbs);
 	r->tables = tcopy;
 	r->limbs = limbs;
-	r->n = n;
+	r->n = tables[0]->n;
 	r->log_n = tables[0]->log_n;
-	r->a = a;
-	r->b = b;
-	r->c = c;
-	r->dev_bytes = req_bytes(r);
+	return r;
+}
+
+/* Queue `r` (id assigned); with operand > 0 the request reads that resident
+ * operand, whose limbs must have the request's (n, q, w).  Returns the id or
+ * -status (r freed). */
+static int64_t enqueue(struct vkhel_server *s, struct srv_req *r, int64_t operand, const char *fn) {
+	int st = VKHEL_OK;
 	pthread_mutex_lock(&s->mu);
 	if (s->stop) {
-		pthread_mutex_unlock(&s->mu);
-		free(tcopy);
-		free(r);
-		return -vkh_fail(NULL, VKHEL_ERR_CANCELLED, "server_submit: server is stopping");
+		st = vkh_fail(NULL, VKHEL_ERR_CANCELLED, "%s: server is stopping", fn);
+	} else if (operand) {
+		struct srv_operand *op = operand > 0 && operand <= s->nops ? s->ops[operand - 1] : NULL;
+		if (!op) {
+			st = vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: unknown or removed operand %lld", fn,
+					(long long) operand);
+		} else if (op->limbs != r->limbs || op->n != r->n) {
+			st = vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: operand %lld has %u limbs of degree %llu", fn,
+					(long long) operand, op->limbs, (unsigned long long) op->n);
+		} else {
+			for (uint32_t k = 0; k < r->limbs && !st; k++)
+				if (op->tables[k]->q != r->tables[k]->q || op->tables[k]->w != r->tables[k]->w)
+					st = vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: limb %u tables differ from operand %lld's",
+							fn, k, (long long) operand);
+		}
+		if (!st) {
+			r->op = op;
+			r->dev_bytes = req_bytes(r);
+		}
 	}
-	if (s->next_id > s->cap_id) {
+	if (!st && s->next_id > s->cap_id) {
 		const int64_t cap = s->cap_id ? 2 * s->cap_id : 4096;
 		struct srv_req **m = realloc(s->by_id, sizeof(*m) * (size_t) cap);
 		if (!m) {
-			pthread_mutex_unlock(&s->mu);
-			free(tcopy);
-			free(r);
-			return -vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "server_submit: host allocation failed");
+			st = vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "%s: host allocation failed", fn);
+		} else {
+			s->by_id = m;
+			s->cap_id = cap;
 		}
-		s->by_id = m;
-		s->cap_id = cap;
 	}
+	if (st) {
+		pthread_mutex_unlock(&s->mu);
+		free(r->tables);
+		free(r);
+		return -st;
+	}
+	if (r->op && !r->upload)
+		r->op->users++;
 	r->id = s->next_id++;
 	s->by_id[r->id - 1] = r;
 	r->t_submit = now_s();
-	if (s->submitted++ == 0)
+	if (!r->upload && s->submitted++ == 0)
 		s->t_first = r->t_submit;
 	if (s->q_tail)
 		s->q_tail->next = r;
@@ -570,6 +689,123 @@ int64_t vkhel_server_submit(struct vkhel_server *s, struct vkhel_ntt_tables *con
 	pthread_cond_signal(&s->cv_work);
 	pthread_mutex_unlock(&s->mu);
 	return r->id;
+}
+
+static int64_t submit_impl(struct vkhel_server *s, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b, int64_t operand, uint64_t *c, const char *fn) {
+	if (!s || !tables || !limbs || !a || (!b && !operand) || !c || !tables[0])
+		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: bad arguments", fn);
+	if (limbs > s->max_limbs)
+		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: %u limbs exceed the micro-batch size %u", fn, limbs,
+				s->max_limbs);
+	int st = check_tables(tables, limbs, fn);
+	if (st)
+		return -st;
+	struct srv_req *r = new_req(tables, limbs);
+	if (!r)
+		return -VKHEL_ERR_OUT_OF_MEMORY;
+	r->a = a;
+	r->b = b;
+	r->c = c;
+	r->dev_bytes = req_bytes(r);
+	return enqueue(s, r, operand, fn);
+}
+
+int64_t vkhel_server_submit(struct vkhel_server *s, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, const uint64_t *b, uint64_t *c) {
+	return submit_impl(s, tables, limbs, a, b, 0, c, "server_submit");
+}
+
+int64_t vkhel_server_submit_operand(struct vkhel_server *s, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *a, int64_t operand, uint64_t *c) {
+	if (operand < 1)
+		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_submit_operand: bad operand id");
+	return submit_impl(s, tables, limbs, a, NULL, operand, c, "server_submit_operand");
+}
+
+int64_t vkhel_server_add_operand(struct vkhel_server *s, struct vkhel_ntt_tables *const *tables, uint32_t limbs,
+		const uint64_t *b, int is_ntt) {
+	const char *fn = "server_add_operand";
+	if (!s || !tables || !limbs || !b || !tables[0])
+		return -vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "%s: bad arguments", fn);
+	int st = check_tables(tables, limbs, fn);
+	if (st)
+		return -st;
+	struct srv_operand *op = calloc(1, sizeof(*op));
+	struct srv_req *r = new_req(tables, limbs);
+	if (!op || !r) {
+		free(op);
+		if (r) {
+			free(r->tables);
+			free(r);
+		}
+		return -vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "%s: host allocation failed", fn);
+	}
+	op->tables = r->tables; /* kept by the operand; the queue entry's copy is not freed twice */
+	r->tables = NULL;
+	op->limbs = limbs;
+	op->n = r->n;
+	op->log_n = r->log_n;
+	op->host = b;
+	op->is_ntt = is_ntt != 0;
+	r->upload = 1;
+	r->op = op;
+	const int64_t id = enqueue(s, r, 0, fn);
+	if (id < 0) {
+		free(op->tables);
+		free(op);
+		return id;
+	}
+	/* the scheduler runs the upload in queue order; wait for it */
+	while ((st = vkhel_server_wait(s, id, 60000)) == VKHEL_ERR_TIMEOUT)
+		;
+	if (st) {
+		free(op->tables);
+		free(op);
+		return -vkh_fail(NULL, st, "%s: upload failed", fn);
+	}
+	op->host = NULL;
+	pthread_mutex_lock(&s->mu);
+	if (s->nops == s->cap_ops) {
+		const int64_t cap = s->cap_ops ? 2 * s->cap_ops : 64;
+		struct srv_operand **m = realloc(s->ops, sizeof(*m) * (size_t) cap);
+		if (!m) {
+			pthread_mutex_unlock(&s->mu);
+			vkcu_free(s->ctx->stream, op->dev);
+			free(op->tables);
+			free(op);
+			return -vkh_fail(NULL, VKHEL_ERR_OUT_OF_MEMORY, "%s: host allocation failed", fn);
+		}
+		s->ops = m;
+		s->cap_ops = cap;
+	}
+	s->ops[s->nops++] = op;
+	const int64_t oid = s->nops;
+	pthread_mutex_unlock(&s->mu);
+	return oid;
+}
+
+int vkhel_server_remove_operand(struct vkhel_server *s, int64_t operand) {
+	if (!s)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_remove_operand: NULL server");
+	pthread_mutex_lock(&s->mu);
+	struct srv_operand *op = operand > 0 && operand <= s->nops ? s->ops[operand - 1] : NULL;
+	if (!op || op->users) {
+		const uint32_t users = op ? op->users : 0;
+		pthread_mutex_unlock(&s->mu);
+		return op ? vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT,
+		                     "server_remove_operand: operand %lld is read by %u queued or running requests",
+		                     (long long) operand, users)
+		          : vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "server_remove_operand: unknown or removed operand %lld",
+		                     (long long) operand);
+	}
+	s->ops[operand - 1] = NULL;
+	pthread_mutex_unlock(&s->mu);
+	/* no request reads it any more: every one that did has finished, kernels included */
+	vkcu_free(s->ctx->stream, op->dev);
+	free(op->tables);
+	free(op);
+	return VKHEL_OK;
 }
 
 int vkhel_server_wait(struct vkhel_server *s, int64_t id, uint32_t timeout_ms) {
@@ -633,7 +869,10 @@ int vkhel_server_cancel(struct vkhel_server *s, int64_t id) {
 	r->state = 2;
 	r->status = VKHEL_ERR_CANCELLED;
 	r->t_done = now_s();
-	s->failed++;
+	if (r->op && !r->upload)
+		r->op->users--;
+	if (!r->upload)
+		s->failed++;
 	pthread_cond_broadcast(&s->cv_done);
 	pthread_mutex_unlock(&s->mu);
 	return VKHEL_OK;
@@ -739,6 +978,16 @@ void vkhel_server_destroy(struct vkhel_server *s) {
 			free(s->by_id[i]);
 		}
 	}
+	for (int64_t i = 0; i < s->nops; i++) {
+		if (s->ops[i]) {
+			vkcu_free(s->ctx->stream, s->ops[i]->dev);
+			free(s->ops[i]->tables);
+			free(s->ops[i]);
+		}
+	}
+	if (s->ctx && s->nops)
+		vkcu_sync(s->ctx->stream);
+	free(s->ops);
 	if (s->ctx)
 		vkhel_ctx_destroy(s->ctx);
 	free(s->slots);
