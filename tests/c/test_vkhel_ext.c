@@ -4,9 +4,10 @@
  * Checks, against a schoolbook negacyclic product and plain C modular
  * arithmetic computed here (unsigned __int128):
  *   - vkhel_vector_polymul and vkhel_vector_polymul_lift (centred elemmod);
+ *   - vkhel_vector_polymul_ntt with NTT(b) from vkhel_vector_forward_transform;
  *   - a committed batch (CUDA graph) of three RNS limb products with a lift;
  *   - an element-wise batch (elemmul, elemgtadd, elemfma_canonical);
- *   - one server request with host operands;
+ *   - one server request with host operands, and one on a resident operand;
  *   - status reporting (vkhel_ctx_last_error) for a bad argument.
  *
  *   test_vkhel_ext N Q0 W0 Q1 W1 Q2 W2
@@ -114,6 +115,12 @@ int main(int argc, char **argv) {
 	for (uint64_t i = 0; ok && i < n; i++)
 		ok = c[i] == centred_mod(ref[i], t_plain, qs[0]);
 	check(ok, "vkhel_vector_polymul_lift (elemmod)");
+	struct vkhel_vector *vbh = vkhel_vector_create(ctx, n);
+	vkhel_vector_forward_transform(vb, vbh, tab[0]);
+	st = vkhel_vector_polymul_ntt(va, vbh, vc, tab[0]);
+	vkhel_vector_download(vc, c, n);
+	check(st == VKHEL_OK && equal(c, ref, n), "vkhel_vector_polymul_ntt (NTT(b) kept)");
+	vkhel_vector_destroy(vbh);
 
 	/* batch of three RNS limbs with the lift, replayed from a CUDA graph */
 	struct vkhel_vector *ba = vkhel_vector_create(ctx, 3 * n), *bb = vkhel_vector_create(ctx, 3 * n),
@@ -168,9 +175,14 @@ int main(int argc, char **argv) {
 		memset(c, 0, 3 * n * 8);
 		const int64_t id = vkhel_server_submit(srv, tab, 3, a, b, c);
 		ok = id > 0 && vkhel_server_wait(srv, id, 10000) == VKHEL_OK && equal(c, ref, 3 * n);
+		const int64_t op = vkhel_server_add_operand(srv, tab, 3, b, 0);
+		memset(c, 0, 3 * n * 8);
+		const int64_t id2 = op > 0 ? vkhel_server_submit_operand(srv, tab, 3, a, op, c) : -1;
+		ok = ok && id2 > 0 && vkhel_server_wait(srv, id2, 10000) == VKHEL_OK && equal(c, ref, 3 * n) &&
+				vkhel_server_remove_operand(srv, op) == VKHEL_OK;
 		vkhel_server_destroy(srv);
 	}
-	check(ok, "vkhel_server (one 3-limb request)");
+	check(ok, "vkhel_server (one 3-limb request, then one on a resident operand)");
 
 	/* status reporting */
 	struct vkhel_vector *small = vkhel_vector_create(ctx, n / 2);
