@@ -958,7 +958,8 @@ void vkhel_server_destroy(struct vkhel_server *s) {
 		vkcu_host_free(sl->host_poly);
 		vkcu_host_free(sl->host_ntt);
 		if (sl->dev_jobs)
-			vkh_dev_free(s->ctx, sl->dev_jobs, 0);
+			vkh_dev_free(s->ctx, sl->dev_jobs,
+					(sizeof(vkcu_poly_job) + 3 * sizeof(vkcu_ntt_job)) * 2 * ((uint64_t) s->max_limbs + 64));
 		free(sl->reqs);
 	}
 	for (int i = 0; i < 3; i++)
