@@ -8,7 +8,8 @@ a and b bit for bit, alone and mixed with plain requests of other and of the
 same degrees (fused CTA and cluster kernels, the composed paths n < 2^8 and
 n >= 2^18, 60- and 63-bit limbs).  Mismatched tables, unknown operands and
 removal while requests still read an operand are refused; an injected
-allocation failure fails the upload alone.
+allocation failure fails the upload alone, or the one request whose buffer
+it was, which then no longer holds the operand.
 """
 import threading
 
@@ -145,3 +146,25 @@ def test_operand_upload_failure_is_reported_and_the_server_goes_on(vk, oracle):
         a, c = _poly(rng, tq, n), np.zeros(2 * n, np.uint64)
         assert srv.wait(srv.submit_operand([t for _, _, t in tq], a, oid, c)) == 0
         _check(oracle, tq, a, b, c)
+
+
+def test_failed_request_releases_its_operand(vk, oracle):
+    """A request on a resident operand whose buffer allocation fails reports
+    out-of-memory; the operand is then read by nobody and can be removed, and
+    the next request on it succeeds."""
+    rng = np.random.default_rng(71)
+    tq = _limbs(vk, 12, 2)
+    n = 1 << 12
+    b = _poly(rng, tq, n)
+    with vk.Server() as srv:
+        oid = srv.add_operand([t for _, _, t in tq], b)
+        a, c = _poly(rng, tq, n), np.zeros(2 * n, np.uint64)
+        vk.fail_allocations(0, 1)
+        try:
+            assert srv.wait(srv.submit_operand([t for _, _, t in tq], a, oid, c)) == 2
+        finally:
+            vk.fail_allocations(0, 0)
+        assert srv.wait(srv.submit_operand([t for _, _, t in tq], a, oid, c)) == 0
+        _check(oracle, tq, a, b, c)
+        srv.remove_operand(oid)
+        assert srv.stats()["failed"] == 1
