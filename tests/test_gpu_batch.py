@@ -71,6 +71,35 @@ def test_ragged_batch_mixes_degrees_and_aliasing(vk, ctx, oracle):
         _check(oracle, qs, ws, a_h, b_h, vc.download(), n)
 
 
+@pytest.mark.parametrize("graph", [True, False])
+def test_scratch_slices_after_tiny_products_stay_aligned(vk, oracle, graph):
+    """Products of n = 2 (3 limbs) need NTT(b) scratch slices of 2 words each;
+    the slices of the larger products after them (n = 2^18 composed, n = 2^14
+    with c aliasing a) must still start on 32-byte boundaries, where their
+    kernels move 16 words at a time with 32-byte vector accesses."""
+    rng = np.random.default_rng(88)
+    with vk.Context() as c:
+        batch = vk.Batch(c)
+        cases = []
+        # unpadded, the slices of n = 2 and 4 (3 limbs each) would end 144 bytes in
+        for log_n, limbs, alias in [(1, 3, False), (18, 2, False), (14, 2, True), (2, 3, True)]:
+            n = 1 << log_n
+            qs = workloads.ntt_primes(n, limbs)
+            ws = [workloads.root_for(n, q) for q in qs]
+            tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+            a_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+            b_h = np.concatenate([workloads.uniform(rng, q, n) for q in qs])
+            va, vb = vk.Vector(c, a_h), vk.Vector(c, b_h)
+            vc = va if alias else vk.Vector(c, limbs * n)
+            batch.add_polymul(tabs, va, vb, vc)
+            cases.append((qs, ws, a_h, b_h, vc, n, tabs, va, vb))
+        batch.commit(graph=graph)
+        batch.run()
+        for qs, ws, a_h, b_h, vc, n, *_ in cases:
+            _check(oracle, qs, ws, a_h, b_h, vc.download(), n)
+        batch.close()
+
+
 def test_batch_raw_device_pointers(vk, ctx, oracle):
     n, limbs = 8192, 2
     qs, ws, a, b = workloads.rns_batch(n, limbs, 1, seed=4)

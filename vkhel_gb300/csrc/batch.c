@@ -260,6 +260,9 @@ int vkhel_batch_add_polymul_raw(struct vkhel_batch *b, struct vkhel_ntt_tables *
 	return add_jobs(b, tables, limbs, a, bb, c, NULL, VKH_JOB_POLYMUL, 0);
 }
 
+/* Words of one job's scratch slice: n rounded up to 32 words (256 bytes). */
+static uint64_t slice_words(uint32_t log_n) { return (((uint64_t) 1 << log_n) + 31) & ~(uint64_t) 31; }
+
 static int cmp_rec(const void *x, const void *y) {
 	const struct job_rec *a = x, *b = y;
 	if (a->kind != b->kind)
@@ -481,7 +484,9 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 	b->dev_bytes = b->scratch_bytes = 0;
 	qsort(b->recs, b->njobs, sizeof(*b->recs), cmp_rec);
 
-	/* classes and scratch slices */
+	/* classes and scratch slices; every slice starts on a 256-byte boundary:
+	 * the kernels of n >= 2^8 move 16 consecutive words with 32-byte vector
+	 * accesses, and slices of n = 1 or 2 words would shift the ones after them */
 	uint64_t scratch_words = 0;
 	b->nclasses = 0;
 	for (uint32_t i = 0; i < b->njobs; i++) {
@@ -503,7 +508,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 		}
 		b->classes[b->nclasses - 1].count++;
 		if (r->needs_scratch)
-			scratch_words += (uint64_t) 1 << r->log_n;
+			scratch_words += slice_words(r->log_n);
 	}
 	if (scratch_words) {
 		b->scratch_bytes = scratch_words * sizeof(uint64_t);
@@ -515,7 +520,7 @@ int vkhel_batch_commit(struct vkhel_batch *b, uint32_t flags) {
 			struct job_rec *r = &b->recs[i];
 			if (r->needs_scratch) {
 				r->job.scratch = (uint64_t *) b->scratch + off;
-				off += (uint64_t) 1 << r->log_n;
+				off += slice_words(r->log_n);
 			}
 		}
 	}
