@@ -44,6 +44,17 @@ uint64_t vkhel_ctx_bytes_in_use(const struct vkhel_ctx *ctx);
 void *vkhel_ctx_stream(struct vkhel_ctx *ctx);
 int vkhel_ctx_sync(struct vkhel_ctx *ctx);
 int vkhel_ctx_sm_count(const struct vkhel_ctx *ctx);
+/* Stream-ordered single calls (off by default; VKHEL_ASYNC=1 turns them on
+ * for new contexts).  On, the transform, element-wise and polymul calls of
+ * this context return once their kernels are enqueued on the context stream,
+ * instead of after they finish as the reference's fence wait makes them:
+ * consecutive calls then run back to back on the GPU.  Results are the same:
+ * every call runs in order on one stream, and the calls that move data to
+ * or from the host (copy_from_host, map, upload, download, dbgprint, dup)
+ * and vkhel_ctx_sync wait for the work before them.  A kernel's device
+ * error is reported by the next call that waits.  Turning it off waits for
+ * the queued work. */
+int vkhel_ctx_set_async(struct vkhel_ctx *ctx, int on);
 /* Kernels launched by this library in this process (graph replays count
  * each kernel node once per replay). */
 uint64_t vkhel_launch_count(void);

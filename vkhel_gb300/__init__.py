@@ -74,6 +74,7 @@ _SIGNATURES = [
     ("vkhel_vector_polymul", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_vector_polymul_noalloc", ctypes.c_int, [vp, vp, vp, vp]),
     ("vkhel_vector_polymul_ntt", ctypes.c_int, [vp, vp, vp, vp]),
+    ("vkhel_ctx_set_async", ctypes.c_int, [vp, ctypes.c_int]),
     ("vkhel_vector_polymul_lift", ctypes.c_int, [vp, vp, vp, vp, vp, u32]),
     ("vkhel_vector_inverse_transform_lift", ctypes.c_int, [vp, vp, vp, vp, u32]),
     ("vkhel_batch_create", vp, [vp]),
@@ -226,6 +227,10 @@ class Context:
 
     def set_budget(self, nbytes):
         _status(self.ptr, lib().vkhel_ctx_set_budget(self.ptr, int(nbytes)))
+
+    def set_async(self, on=True):
+        """vkhel_ctx_set_async: single calls return once their kernels are enqueued."""
+        _status(self.ptr, lib().vkhel_ctx_set_async(self.ptr, 1 if on else 0))
 
     @property
     def bytes_in_use(self):

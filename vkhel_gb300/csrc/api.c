@@ -111,6 +111,7 @@ struct vkhel_ctx *vkhel_ctx_create() {
 		return NULL;
 	}
 	ctx->strict = env_flag("VKHEL_STRICT");
+	ctx->async = env_flag("VKHEL_ASYNC");
 	const char *dev = getenv("VKHEL_DEVICE");
 	ctx->device = dev ? atoi(dev) : 0;
 	const char *budget = getenv("VKHEL_DEVICE_BUDGET");
@@ -160,6 +161,18 @@ void vkhel_ctx_clear_error(struct vkhel_ctx *ctx) {
 	}
 	tls_error = 0;
 	tls_msg[0] = 0;
+}
+
+int vkhel_ctx_set_async(struct vkhel_ctx *ctx, int on) {
+	if (!ctx)
+		return vkh_fail(NULL, VKHEL_ERR_INVALID_ARGUMENT, "set_async: NULL context");
+	if (ctx->async && !on) { /* back to blocking calls: nothing may still be queued */
+		const int e = vkcu_sync(ctx->stream);
+		ctx->async = 0;
+		return vkh_cuda(ctx, e, "set_async: synchronize");
+	}
+	ctx->async = on != 0;
+	return VKHEL_OK;
 }
 
 int vkhel_ctx_set_budget(struct vkhel_ctx *ctx, uint64_t bytes) {
@@ -386,9 +399,11 @@ int vkh_check_mod(struct vkhel_ctx *ctx, const char *op, uint64_t mod) {
 	return VKHEL_OK;
 }
 
+/* End of a single call: wait for its kernels as the reference waits on its
+ * fence (src/vector.c:326), unless the context is stream-ordered. */
 static int finish(struct vkhel_ctx *ctx, int launch_err, const char *op) {
 	int e = launch_err;
-	if (!e)
+	if (!e && !ctx->async)
 		e = vkcu_sync(ctx->stream);
 	return vkh_cuda(ctx, e, op);
 }

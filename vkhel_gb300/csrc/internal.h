@@ -38,6 +38,7 @@ struct vkhel_ctx {
 	uint64_t budget;           /* 0 = unlimited */
 	uint64_t in_use;
 	int strict;                /* abort on error like the reference's asserts */
+	int async;                 /* single calls return once enqueued (vkhel_ctx_set_async) */
 	int last_error;
 	char last_msg[256];
 	struct vkh_devtab *tabs;
