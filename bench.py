@@ -236,7 +236,8 @@ def serving_sweep(vk, torch, orc, rates=(1000, 4000, 16000, None), seconds=1.0, 
     """Poisson arrivals of polymul requests (n = 2^k, k uniform in 12..17,
     limbs uniform in 1..24, operands uniform mod each prime, seed 4) into a
     vkhel server with a 40 GB budget; `None` = all requests at once
-    (saturation).  The requests cycle through `payloads` distinct requests of
+    (saturation); each rate runs three times and the run with the median p99
+    is reported.  The requests cycle through `payloads` distinct requests of
     that distribution (pinned host operands; fresh operands for every one of
     the thousands of requests would need tens of GB of host memory).  Returns
     the per-rate results and the plain per-call path; every payload's last
@@ -294,9 +295,19 @@ def serving_sweep(vk, torch, orc, rates=(1000, 4000, 16000, None), seconds=1.0, 
                     "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
                     "micro_batches": st["batches"], "failed": fails}
 
+        def median_of(rate, submit, runs=3):
+            """`runs` back-to-back runs at one rate; the run with the median
+            p99 is reported, every run's figures beside it (the hosts are
+            shared, and one run in several has shown a stall of tens of ms)."""
+            rs = [drive(rate, submit) for _ in range(runs)]
+            pick = sorted(rs, key=lambda r: r["p99_ms"])[runs // 2]
+            rep = dict(pick)
+            rep["runs"] = [{k: r[k] for k in ("achieved_req_per_s", "p50_ms", "p99_ms", "max_ms")} for r in rs]
+            return rep
+
         plain = lambda i: srv.submit(pay[i][2], pay[i][3], pay[i][4], pay[i][5])
         for rate in rates:
-            out["rates"].append(drive(rate, plain))
+            out["rates"].append(median_of(rate, plain))
         # resident operands: every payload's b uploaded once (transformed on
         # the device) and kept; its requests bring a only
         oids = [srv.add_operand(p_[2], p_[4]) for p_ in pay]
@@ -306,7 +317,7 @@ def serving_sweep(vk, torch, orc, rates=(1000, 4000, 16000, None), seconds=1.0, 
         out["resident_operands"] = {
             "workload": "the same payloads, each b kept on the server as a resident operand "
                         "(vkhel_server_add_operand, transformed on the device once); requests upload a only",
-            "rates": [drive(rate, resident) for rate in (1000, 4000, None)]}
+            "rates": [median_of(rate, resident) for rate in (1000, 4000, None)]}
         for o in oids:
             srv.remove_operand(o)
     # every payload's result (its last run) against the oracle, all limbs
