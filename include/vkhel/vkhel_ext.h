@@ -278,8 +278,11 @@ void vkhel_elem_batch_destroy(struct vkhel_elem_batch *batch);
  * from tuning/gb300.txt beside the package (written by vkhel_gb300.autotune).
  * Family VKHEL_TUNE_BATCH, log_n 0: 1 = run the degree classes of a batch on
  * concurrent streams; log_n 1: 1 = never split a few n = 2^12 .. 2^16 jobs
- * (at most one per 8 SMs, e.g. a single call) over 8-CTA clusters (the
- * default, 0, splits them). */
+ * (at most one per 8 SMs, e.g. a single call) over clusters (the default, 0,
+ * splits them: over 16 CTAs for n >= 2^14 with at most one job per 16 SMs,
+ * otherwise over 8); log_n 2: 1 = run a ragged batch of fused products of
+ * 2^12 .. 2^16 as one persistent launch; log_n 3: 1 = split over 8 CTAs
+ * only. */
 enum vkhel_tune_family {
 	VKHEL_TUNE_POLYMUL = 0,
 	VKHEL_TUNE_FORWARD = 1,

@@ -51,11 +51,16 @@ def test_every_variant_matches_oracle(vk, ctx, oracle, log_n):
 
 
 @pytest.mark.parametrize("log_n", [12, 13, 14, 15, 16])
-@pytest.mark.parametrize("split", [0, 1])
+@pytest.mark.parametrize("split", [0, 1, 2])
 def test_single_calls_split_or_not_are_exact(vk, ctx, oracle, log_n, split):
-    """A single call of n = 2^12 .. 2^16 runs on an 8-CTA cluster (2^9 .. 2^13-word
-    sub-blocks) unless the split is switched off; both give the oracle's words."""
+    """A single call of n = 2^12 .. 2^16 runs on a cluster -- 16 CTAs with
+    2^10 .. 2^12-word sub-blocks from n = 2^14 (split = 0), 8 CTAs with 2^9 ..
+    2^13-word ones below or with tuning entry (3, 3) = 1 (split = 2) -- unless
+    the split is switched off (split = 1); all give the oracle's words."""
     L = vk.lib()
+    saved16 = L.vkhel_tune_get(3, 3)
+    L.vkhel_tune_set(3, 3, 1 if split == 2 else 0)
+    split = 1 if split == 1 else 0
     n = 1 << log_n
     q = workloads.ntt_primes(n, 1, bound=1 << 62)[0]
     w = workloads.root_for(n, q)
@@ -85,6 +90,7 @@ def test_single_calls_split_or_not_are_exact(vk, ctx, oracle, log_n, split):
         np.testing.assert_array_equal(c.download(), ref)
     finally:
         L.vkhel_tune_set(3, 1, saved)
+        L.vkhel_tune_set(3, 3, saved16)
 
 
 @pytest.mark.parametrize("concurrent", [0, 1])

@@ -236,8 +236,16 @@ static bool jobs_aligned(const vkcu_ntt_job* jobs, const vkcu_ntt_job* one) {
 // each runs on a cluster of 8 CTAs with 2^9 .. 2^13-word sub-blocks instead
 // of one CTA (n <= 2^14) or a cluster of 2 / 4 CTAs (n = 2^15 / 2^16), so it
 // uses 8 SMs.  Tuning entry (family 3, log_n 1) = 1 turns this off.
-static bool split_small(int njobs, uint32_t log_n, int sms) {
-  return log_n >= 12 && log_n <= 16 && (long)njobs * 8 <= (long)sms && vkh_variant(3, 1) == 0;
+// Cluster size (log2) for a few jobs of n = 2^12 .. 2^16, 0 for none: 8
+// CTAs when there is at most one job per 8 SMs; 16 for a single call (one
+// job passed by value) of n >= 2^14 (tuning entry (3, 3) = 1 keeps it on 8).
+// Batches and server micro-batches keep 8: their classes run beside other
+// kernels, and a 16-CTA cluster can only start once 16 SMs of one GPC are
+// free at the same time.
+static int split_small(int njobs, uint32_t log_n, int sms, bool single) {
+  if (log_n < 12 || log_n > 16 || vkh_variant(3, 1) != 0) return 0;
+  if (single && log_n >= 14 && (long)njobs * 16 <= (long)sms && vkh_variant(3, 3) == 0) return 4;
+  return (long)njobs * 8 <= (long)sms ? 3 : 0;
 }
 
 extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njobs, const vkcu_ntt_job* one,
@@ -254,7 +262,12 @@ extern "C" int vkcu_ntt_forward(void* stream, const vkcu_ntt_job* jobs, int njob
     if (log_n <= (uint32_t)kMaxCta) return fwd_cta_wide(st, jobs, njobs, o, (int)log_n, 0, sms);
     if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta);
   } else {
-    if (split_small(njobs, log_n, sms)) return fwd_cluster(st, jobs, njobs, o, 3, (int)log_n - 3);
+    if (const int lc = split_small(njobs, log_n, sms, jobs == nullptr)) {
+      const int e = fwd_cluster(st, jobs, njobs, o, lc, (int)log_n - lc);
+      // a GPU that cannot host 16-CTA clusters: the set-up refuses before any launch
+      return e == (int)cudaErrorInvalidConfiguration && lc == 4 ? fwd_cluster(st, jobs, njobs, o, 3, (int)log_n - 3)
+                                                                : e;
+    }
     if (log_n <= (uint32_t)kMaxCta) return fwd_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant_jobs(1, (int)log_n, njobs, sms));
     if (log_n <= (uint32_t)kMaxCluster) return fwd_cluster(st, jobs, njobs, o, (int)log_n - kMaxCta, kMaxCta);
   }
@@ -292,8 +305,11 @@ extern "C" int vkcu_ntt_inverse_lift(void* stream, const vkcu_ntt_job* jobs, int
     return inv_cta_wide(st, jobs, njobs, o, (int)log_n, 0, sms, lp);
   } else if (wide && log_n <= (uint32_t)kMaxCluster) {
     return inv_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta, lp);
-  } else if (!wide && split_small(njobs, log_n, sms)) {
-    return inv_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
+  } else if (!wide && split_small(njobs, log_n, sms, jobs == nullptr)) {
+    const int lc = split_small(njobs, log_n, sms, jobs == nullptr);
+    const int e = inv_cluster(st, jobs, njobs, o, lc, (int)log_n - lc, lp);
+    return e == (int)cudaErrorInvalidConfiguration && lc == 4 ? inv_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp)
+                                                              : e;
   } else if (!wide && log_n <= (uint32_t)kMaxCta) {
     if (lifted) return inv_cta_lift(st, jobs, njobs, o, (int)log_n, sms, *lift);
     return inv_cta(st, jobs, njobs, o, (int)log_n, 0, sms, vkh_variant_jobs(2, (int)log_n, njobs, sms));
@@ -332,7 +348,11 @@ extern "C" int vkcu_polymul_lift(void* stream, const vkcu_poly_job* jobs, int nj
     if (log_n <= (uint32_t)kMaxCta) return poly_cta_wide(st, jobs, njobs, o, (int)log_n, sms, lp);
     return poly_cluster_wide(st, jobs, njobs, o, (int)log_n - kMaxCta, lp);
   }
-  if (split_small(njobs, log_n, sms)) return poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp);
+  if (const int lc = split_small(njobs, log_n, sms, jobs == nullptr)) {
+    const int e = poly_cluster(st, jobs, njobs, o, lc, (int)log_n - lc, lp);
+    return e == (int)cudaErrorInvalidConfiguration && lc == 4 ? poly_cluster(st, jobs, njobs, o, 3, (int)log_n - 3, lp)
+                                                              : e;
+  }
   if (log_n <= (uint32_t)kMaxCta) {
     if (lp) return poly_cta_lift(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms), *lp);
     return poly_cta(st, jobs, njobs, o, (int)log_n, sms, vkh_variant_jobs(0, (int)log_n, njobs, sms));

@@ -279,12 +279,17 @@ static int launch_cluster(cudaStream_t st, int njobs, Args... args) {
   const int dev = current_device();
   const bool cached = dev >= 0 && dev < 32;
   int max_clusters = cached ? setup.per_dev[dev].load(std::memory_order_acquire) : 0;
+  if (max_clusters < 0) return (int)cudaErrorInvalidConfiguration;  // no such cluster fits this GPU
   cudaError_t e = cudaSuccess;
   if (max_clusters < 1) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM_BYTES);
+    if (e == cudaSuccess && C > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg);
     if (e != cudaSuccess) return (int)e;
-    if (max_clusters < 1) return (int)cudaErrorInvalidConfiguration;
+    if (max_clusters < 1) {
+      if (cached) setup.per_dev[dev].store(-1, std::memory_order_release);
+      return (int)cudaErrorInvalidConfiguration;
+    }
     if (cached) setup.per_dev[dev].store(max_clusters, std::memory_order_release);
   }
   const int nclusters = njobs < max_clusters ? njobs : max_clusters;
@@ -302,7 +307,9 @@ using Small11 = Shape<11, 16>;
 using Small12 = Shape<12, 16>;
 using Small13 = Shape<13, 32>;
 
-// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 9 .. 13 with logc = 3).
+// logc: cluster size 2^logc; logs: sub-block size 2^logs (14, or 9 .. 13
+// with logc = 3, or 10 .. 12 with logc = 4: n = 2^14 .. 2^16 on 16 CTAs, a
+// cluster size the GPU allows on request).
 #define VK_CLUSTER_SHAPES(X)                                 \
   switch (logc * 32 + logs) {                                \
     case 1 * 32 + 14: return X(1, SubShape);                 \
@@ -313,6 +320,9 @@ using Small13 = Shape<13, 32>;
     case 3 * 32 + 11: return X(3, Small11);                  \
     case 3 * 32 + 12: return X(3, Small12);                  \
     case 3 * 32 + 13: return X(3, Small13);                  \
+    case 4 * 32 + 10: return X(4, Small10);                  \
+    case 4 * 32 + 11: return X(4, Small11);                  \
+    case 4 * 32 + 12: return X(4, Small12);                  \
     default: return (int)cudaErrorInvalidValue;              \
   }
 
