@@ -27,6 +27,8 @@ the device so that a profiler capture of one launch ends quickly.
                 k_ntt_fwd<14,..,Mod63>, k_ntt_fwd_cluster<2, Shape<14,32,1,Mod63>>
   ntt_operand   256 polymuls of n = 2^14 with b given as NTT(b)  k_polymul<14,..,true> (the
                 epilogue instantiation, no steps)
+  single_call_n65536  one polymul and one forward transform of n = 2^16 as single calls
+                k_polymul_cluster<4, Shape<12,16>>, k_ntt_fwd_cluster<4, ..> (16-CTA clusters)
 """
 import argparse
 import sys
@@ -141,6 +143,18 @@ def case_ntt_operand(ctx):
                        b_ntt=True)
     bt.commit(graph=True)
     return bt.launch, (bt, a, b, bn, c, tabs)
+
+
+def case_single_call_n65536(ctx):
+    n = 1 << 16
+    qs, tabs = _tabs(n, 1)
+    a, b = _operands(ctx, n, qs, 1, 1), _operands(ctx, n, qs, 1, 2)
+    c = vk.Vector(ctx, n)
+
+    def calls():
+        vk.polymul(a, b, c, tabs[0])
+        vk.forward_transform(a, c, tabs[0])
+    return calls, (a, b, c, tabs)
 
 
 def case_ragged_single(ctx):
