@@ -643,6 +643,32 @@ def ntt_operand_batch(vk, ctx, torch, orc, pairs=4 * PAIRS):
             "checked_against_oracle": f"all {pairs * LIMBS} limb products (device) and the 256 of every context (e2e)"}
 
 
+def call_latency(vk, ctx, torch, orc, reps=2000):
+    """Per-call latency of the public C API from a C program
+    (tests/c/call_latency.c, compiled here with gcc against libvkhel.so):
+    elemgtadd on one word, forward n = 4096, forward / inverse / polymul
+    n = 16384, forward / polymul n = 65536, blocking as the reference's calls
+    are and stream-ordered (vkhel_ctx_set_async); best of five loops of
+    `reps` calls each, host monotonic clock, one sync at the end of a loop."""
+    import subprocess
+    import tempfile
+    from vkhel_gb300 import LIB_PATH, workloads
+    libdir = os.path.dirname(LIB_PATH)
+    args = []
+    for n in (16384, 4096, 65536):
+        q = workloads.ntt_primes(n, 1)[0]
+        args += [str(q), str(workloads.root_for(n, q))]
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(tmp, "call_latency")
+        subprocess.run(["gcc", "-std=gnu11", "-O2", "-I", os.path.join(ROOT, "include", "vkhel"),
+                        os.path.join(ROOT, "tests", "c", "call_latency.c"), "-o", exe, "-L", libdir, "-lvkhel",
+                        f"-Wl,-rpath,{libdir}"], check=True)
+        r = subprocess.run([exe] + args + [str(reps)], capture_output=True, text=True, check=True)
+    out = json.loads(r.stdout)
+    out["program"] = "tests/c/call_latency.c"
+    return out
+
+
 def elementwise_batch(vk, ctx, torch, orc, jobs=2048, seed=6):
     """2048 ragged element-wise jobs (lengths uniform in 1 .. 2^17 words, ops
     cycling through elemfma, elemmul, elemmod, elemgtsub, elemgtadd, 61-bit
@@ -794,6 +820,7 @@ EXTRAS = {"single_limb_batch": single_limb_batch, "ragged_batch": ragged_batch,
           "transform_batch": transform_batch,
           "standalone_ops": standalone_ops,
           "lift_epilogue": lift_epilogue, "ntt_operand_batch": ntt_operand_batch,
+          "call_latency": call_latency,
           "elementwise_batch": elementwise_batch,
           "device_twiddles": device_twiddles}
 

@@ -103,6 +103,43 @@ def test_c_extension_program_checks_pass(vk, tmp_path):
     assert "0 checks failed" in r.stdout
 
 
+LAT_SRC = os.path.join(ROOT, "tests", "c", "call_latency.c")
+
+
+def _latency_args():
+    from vkhel_gb300 import workloads
+    out = []
+    for n in (16384, 4096, 65536):
+        q = workloads.ntt_primes(n, 1)[0]
+        out += [str(q), str(workloads.root_for(n, q))]
+    return out
+
+
+def _build_latency(tmp_path):
+    from vkhel_gb300 import LIB_PATH
+    exe = str(tmp_path / "call_latency")
+    libdir = os.path.dirname(LIB_PATH)
+    subprocess.run(["gcc", "-std=gnu11", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include", "vkhel"),
+                    LAT_SRC, "-o", exe, "-L", libdir, "-lvkhel", f"-Wl,-rpath,{libdir}"], check=True)
+    return exe
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_call_latency_program_links_and_reports_no_device(vk, tmp_path):
+    r = subprocess.run([_build_latency(tmp_path)] + _latency_args(), capture_output=True, text=True)
+    assert r.returncode == 77
+
+
+@pytest.mark.gpu
+def test_call_latency_program_reports_every_call(vk, tmp_path):
+    import json
+    r = subprocess.run([_build_latency(tmp_path)] + _latency_args() + ["20"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    d = json.loads(r.stdout)
+    for mode in ("blocking_us", "stream_ordered_us"):
+        assert len(d[mode]) == 7 and all(v > 0 for v in d[mode].values())
+
+
 # The reference's own programs (test/vector.c, examples/example.c) include
 # only its public header.  Where the reference's sources are present (they
 # are not on GPU machines) they must compile against include/vkhel/vkhel.h
