@@ -225,12 +225,12 @@ def test_transform_rejects_unsupported(vk, ctx):
         vk.forward_transform(a, a, t)  # vector shorter than n
 
 
-@pytest.mark.parametrize("log_n", [17, 22, 24])
+@pytest.mark.parametrize("log_n", [17, 22, 24, 26])
 def test_round_trip_largest_degree(vk, ctx, log_n):
     n = 1 << log_n
     # 62- and 63-bit tables are built on the host (63-bit: one extended-Euclid
     # inverse per entry, as the reference does), seconds at 2^24
-    for bits in (40, 60, 62, 63) if log_n < 24 else (40, 60):
+    for bits in (40, 60, 62, 63) if log_n < 24 else (40, 60) if log_n < 26 else (60,):
         q, w = ntt_params(n, bits)
         t = vk.NttTables(n, q, w)
         a_h = workloads.uniform(np.random.default_rng(bits), q, n)
@@ -239,6 +239,28 @@ def test_round_trip_largest_degree(vk, ctx, log_n):
         assert (v.download() < q).all()
         vk.inverse_transform(v, v, t)
         np.testing.assert_array_equal(v.download(), a_h)
+
+
+@pytest.mark.parametrize("log_n", [18, 22, 26])
+def test_polymul_by_a_monomial_is_a_negacyclic_rotation(vk, ctx, log_n):
+    """At degrees the oracle is too slow for, the product with X^k is exactly
+    known: a rotated by k with the k wrapped words negated mod q (X^n = -1).
+    Checked through the composed path (n >= 2^18) up to the largest degree."""
+    n = 1 << log_n
+    q, w = ntt_params(n, 60)
+    rng = np.random.default_rng(log_n)
+    t = vk.NttTables(n, q, w)
+    a_h = workloads.uniform(rng, q, n)
+    for k in (1, int(rng.integers(2, n))):
+        b_h = np.zeros(n, np.uint64)
+        b_h[k] = 1
+        a, b, c = vk.Vector(ctx, a_h), vk.Vector(ctx, b_h), vk.Vector(ctx, n)
+        vk.polymul(a, b, c, t)
+        want = np.empty(n, np.uint64)
+        want[k:] = a_h[:n - k]
+        tail = a_h[n - k:]
+        want[:k] = np.where(tail == 0, np.uint64(0), np.uint64(q) - tail)
+        np.testing.assert_array_equal(c.download(), want, err_msg=f"X^{k}")
 
 
 @pytest.mark.parametrize("bits", [60, 63])
