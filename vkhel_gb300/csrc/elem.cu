@@ -15,6 +15,8 @@
 // one scalar tail element is handled by one thread.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "elem_ops.cuh"
 #include "kernels.h"
 
@@ -22,14 +24,22 @@ namespace vk {
 
 // B == nullptr for unary operations.  Each thread moves P 16-byte pairs of
 // every operand per iteration (2 for binary ops, 4 for unary ones, so both
-// keep about the same bytes in flight), all loads issued before the first
-// store, and the next iteration's loads issued before this one's arithmetic
-// (2-3.4 % faster for the ops with multiplies, 0.8 % slower for elemgtadd);
-// lanes past the end re-read the last pair and store nothing.
+// keep about the same bytes in flight; 8 for the multiply-free unary ops,
+// whose arithmetic hides no load latency: elemgtadd 0.909 -> 0.937 of the
+// copy bandwidth, while 8 made the reductions of elemgtsub / elemmod 8 %
+// and elemfma's 4 % slower), all loads issued before the first store, and
+// the next iteration's loads issued before this one's arithmetic (2-3.4 %
+// faster for the ops with multiplies); lanes past the end re-read the last
+// pair and store nothing.
+template <class Op>
+constexpr int pairs_per_thread(bool bin) {
+  return bin ? 2 : (std::is_same<Op, OpGtAdd>::value || std::is_same<Op, OpModTwo>::value) ? 8 : 4;
+}
+
 template <class Op, bool BIN>
 __global__ void __launch_bounds__(256) k_elementwise(u64* __restrict__ res, const u64* a, const u64* b, u64 len,
                                                      Op op) {
-  constexpr int P = BIN ? 2 : 4;
+  constexpr int P = pairs_per_thread<Op>(BIN);
   const u64 pairs = len >> 1;
   const u64 step = (u64)gridDim.x * blockDim.x * P;
   const u64 first = (u64)blockIdx.x * blockDim.x * P;
@@ -94,7 +104,7 @@ static int launch(void* stream, uint64_t* res, const uint64_t* a, const uint64_t
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_sms <= 0) g_sms = 1;
   }
-  const u64 per_block = 256 * (b ? 2 : 4);  // pairs a block moves per iteration
+  const u64 per_block = 256 * (u64)(b ? pairs_per_thread<Op>(true) : pairs_per_thread<Op>(false));  // pairs a block moves per iteration
   const u64 want = ((len + 1) / 2 + per_block - 1) / per_block;
   auto* r = reinterpret_cast<u64*>(res);
   auto* x = reinterpret_cast<const u64*>(a);
