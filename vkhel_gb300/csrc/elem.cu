@@ -23,17 +23,20 @@
 namespace vk {
 
 // B == nullptr for unary operations.  Each thread moves P 16-byte pairs of
-// every operand per iteration (2 for binary ops, 4 for unary ones, so both
-// keep about the same bytes in flight; 8 for the multiply-free unary ops,
-// whose arithmetic hides no load latency: elemgtadd 0.909 -> 0.937 of the
-// copy bandwidth, while 8 made the reductions of elemgtsub / elemmod 8 %
-// and elemfma's 4 % slower), all loads issued before the first store, and
+// every operand per iteration, all loads issued before the first store, and
 // the next iteration's loads issued before this one's arithmetic (2-3.4 %
 // faster for the ops with multiplies); lanes past the end re-read the last
-// pair and store nothing.
+// pair and store nothing.  P per op, measured on 2^27-word vectors (fraction
+// of the copy bandwidth per public call): the multiply-free unary ops take 8
+// (elemgtadd 0.909 with 4 -> 0.94), the unary ops with a reduction or a
+// Shoup product 2 (elemgtsub / elemmod 0.87-0.89 with 4 -> 0.92; 8 made
+// them 0.80), elemmul 1 (0.937 with 2 -> 0.954), the fused multiply-adds 2
+// (elemfma 0.96; 4 made it 0.925).
 template <class Op>
 constexpr int pairs_per_thread(bool bin) {
-  return bin ? 2 : (std::is_same<Op, OpGtAdd>::value || std::is_same<Op, OpModTwo>::value) ? 8 : 4;
+  if (bin) return std::is_same<Op, OpMul>::value ? 1 : 2;
+  if (std::is_same<Op, OpGtAdd>::value || std::is_same<Op, OpModTwo>::value) return 8;
+  return 2;
 }
 
 template <class Op, bool BIN>
