@@ -5,6 +5,7 @@
 // (`wide`: 2^62 <= q < 2^63).  The CTA-resident kernels are in
 // ntt_core.cuh with one launcher per family (ntt_fwd.cu, ntt_inv.cu,
 // ntt_poly.cu).
+#include "elem_ops.cuh"
 #include "ntt_core.cuh"
 
 namespace vk {
@@ -417,25 +418,41 @@ extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs,
 // Pointwise step of a composed polymul: c = c * scratch mod q over njobs
 // jobs of n words each, the word the reference's elemmul stores: c is a
 // canonical NTT output, scratch one too or the caller's NTT(b), reduced as
-// elemmul reduces its operands.
+// elemmul reduces its operands.  A block takes chunks of up to 2048 words of
+// one job (the job's constants loaded once per chunk, not per word), each
+// thread two 16-byte pairs of c and of scratch per round, loads first.
 template <class M>
-__global__ void k_pointwise(const vkcu_poly_job* __restrict__ jobs, int njobs, int log_n) {
-  const long n = 1L << log_n;
-  const long total = (long)njobs * n;
-  for (long w = blockIdx.x * (long)blockDim.x + threadIdx.x; w < total; w += (long)gridDim.x * blockDim.x) {
-    const vkcu_poly_job job = jobs[w >> log_n];
-    const long i = w & (n - 1);
+__global__ void __launch_bounds__(256) k_pointwise(const vkcu_poly_job* __restrict__ jobs, int njobs, int log_n) {
+  const int lw = log_n < 11 ? log_n : 11;  // log2 of the words of a chunk
+  const long cpj = 1L << (log_n - lw);    // chunks per job
+  const long total = (long)njobs * cpj;
+  const int pairs = 1 << (lw - 1);         // n >= 2
+  for (long ch = blockIdx.x; ch < total; ch += gridDim.x) {
+    const vkcu_poly_job job = jobs[ch >> (log_n - lw)];
     const Tw t = load_tw(job.tw);
-    u64* c = reinterpret_cast<u64*>(job.c);
-    const u64 x = c[i], y = ref_reduce64_maybe(reinterpret_cast<const u64*>(job.scratch)[i], t.q, t.mu, t.qbits);
-    c[i] = M::product_out(x, y, t);
+    const long base = (ch & (cpj - 1)) << lw;
+    u64* c = reinterpret_cast<u64*>(job.c) + base;
+    const u64* y = reinterpret_cast<const u64*>(job.scratch) + base;
+    auto prod = [&](u64 x, u64 b) { return M::product_out(x, ref_reduce64_maybe(b, t.q, t.mu, t.qbits), t); };
+    for (int p = (int)threadIdx.x; p < pairs; p += 2 * (int)blockDim.x) {
+      const int p1 = p + (int)blockDim.x;
+      const bool two = p1 < pairs;
+      const ulonglong2 x0 = ld2(c + 2 * p), y0 = ld2(y + 2 * p);
+      ulonglong2 x1 = x0, y1 = y0;
+      if (two) {
+        x1 = ld2(c + 2 * p1);
+        y1 = ld2(y + 2 * p1);
+      }
+      st2(c + 2 * p, prod(x0.x, y0.x), prod(x0.y, y0.y));
+      if (two) st2(c + 2 * p1, prod(x1.x, y1.x), prod(x1.y, y1.y));
+    }
   }
 }
 
 extern "C" int vkcu_pointwise(void* stream, const vkcu_poly_job* jobs, int njobs, uint32_t log_n, int wide, int sms) {
-  if (njobs < 1 || !jobs) return (int)cudaErrorInvalidValue;
-  const long work = (long)njobs << log_n;
-  long blocks = (work + 255) / 256;
+  if (njobs < 1 || !jobs || log_n < 1) return (int)cudaErrorInvalidValue;
+  const long chunks = (long)njobs << (log_n > 11 ? log_n - 11 : 0);
+  long blocks = chunks;
   if (blocks > (long)sms * 8) blocks = (long)sms * 8;
   if (wide)
     k_pointwise<Mod63><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, (int)log_n);
