@@ -20,7 +20,7 @@ the device so that a profiler capture of one launch ends quickly.
   wide_polymul  256 polymuls of n = 2^14, 63-bit primes         k_polymul<14,..,Mod63>
   cluster_polymul  64 polymuls of n = 2^16 (single-limb batch)  k_polymul_cluster<2,..>
   ragged_single  256 ragged instances, n = 2^12..2^16, as one launch   k_polymul_ragged
-  elementwise   elemgtsub / elemmod / elemgtadd / elemfma on 2^25 words   k_elementwise<...>
+  elementwise   elemgtsub / elemmod / elemgtadd / elemfma / elemmul on 2^25 words   k_elementwise<...>
   elementwise_rest  elemmod mod 2, elemfma_canonical, the n^-1 scaling and lift of
                 the words past n of an inverse transform      k_elementwise<...>, k_lift_range
   wide_transforms  1024 forward transforms of n = 2^14 and 64 of n = 2^16, 63-bit primes
@@ -185,6 +185,7 @@ def case_elementwise(ctx):
         vk.elemmod(a, r, 65537, q)
         vk.elemgtadd(a, r, q // 2, 17)
         vk.elemfma(a, b, r, 12345, q)
+        vk.elemmul(a, b, r, q)
     return run, (a, b, r)
 
 
