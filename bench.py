@@ -658,12 +658,15 @@ def call_latency(vk, ctx, torch, orc, reps=2000):
     for n in (16384, 4096, 65536):
         q = workloads.ntt_primes(n, 1)[0]
         args += [str(q), str(workloads.root_for(n, q))]
-    with tempfile.TemporaryDirectory() as tmp:
-        exe = os.path.join(tmp, "call_latency")
-        subprocess.run(["gcc", "-std=gnu11", "-O2", "-I", os.path.join(ROOT, "include", "vkhel"),
-                        os.path.join(ROOT, "tests", "c", "call_latency.c"), "-o", exe, "-L", libdir, "-lvkhel",
-                        f"-Wl,-rpath,{libdir}"], check=True)
-        r = subprocess.run([exe] + args + [str(reps)], capture_output=True, text=True, check=True)
+    try:
+        with tempfile.TemporaryDirectory() as tmp:
+            exe = os.path.join(tmp, "call_latency")
+            subprocess.run(["gcc", "-std=gnu11", "-O2", "-I", os.path.join(ROOT, "include", "vkhel"),
+                            os.path.join(ROOT, "tests", "c", "call_latency.c"), "-o", exe, "-L", libdir, "-lvkhel",
+                            f"-Wl,-rpath,{libdir}"], check=True, capture_output=True)
+            r = subprocess.run([exe] + args + [str(reps)], capture_output=True, text=True, check=True)
+    except (OSError, subprocess.CalledProcessError) as e:  # no C compiler, or the program failed
+        return {"unavailable": f"{type(e).__name__}: {e}"}
     out = json.loads(r.stdout)
     out["program"] = "tests/c/call_latency.c"
     return out
