@@ -488,6 +488,18 @@ def ragged_batch(vk, ctx, torch, orc):
             "kernels_per_batch": kernels, "checked_against_oracle": f"all {limbs_total} limb products"}
 
 
+def guarded(what, fn, *args):
+    """A secondary measurement that fails (an oracle mismatch included) is
+    reported in its place in the JSON line, with the traceback on stderr, and
+    does not take the headline line with it."""
+    import traceback
+    try:
+        return fn(*args)
+    except Exception as e:  # noqa: BLE001 -- every failure is reported, none swallowed silently
+        traceback.print_exc()
+        return {"error": f"{what}: {type(e).__name__}: {e}"}
+
+
 def extra_configs(vk, torch):
     """The secondary measurements (each also runnable alone: --extra NAME)."""
     from oracle import pyoracle
@@ -495,7 +507,7 @@ def extra_configs(vk, torch):
     out = {}
     for name, fn in EXTRAS.items():
         ctx = vk.Context()
-        out[name] = fn(vk, ctx, torch, orc)
+        out[name] = guarded(name, fn, vk, ctx, torch, orc)
         ctx.close()
     return out
 
@@ -1140,10 +1152,10 @@ def main():
     for c in ctxs:
         c.close()
     if rank == 0 and not args.no_serve:
-        result["serving"] = serving_sweep(vk, torch, orc)
+        result["serving"] = guarded("serving", serving_sweep, vk, torch, orc)
         result.update(extra_configs(vk, torch))
     if rank == 0 and not args.no_cpu:
-        result["cpu_baseline"] = cpu_baseline_sample(qs, ws, a_h, b_h)
+        result["cpu_baseline"] = guarded("cpu_baseline", cpu_baseline_sample, qs, ws, a_h, b_h)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if dist:
