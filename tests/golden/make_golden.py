@@ -144,6 +144,14 @@ def reference_tables():
         (4096, _ntt_prime(4096, 1 << 63, down=True), None),
         (16384, _ntt_prime(16384, 1 << 62, down=False), None),
         (1 << 20, _ntt_prime(1 << 20, 1 << 60, down=True), None),
+        # the smallest degree, a 31-bit prime, the largest one-launch degree,
+        # a degree past 2^20, and a w that is not a primitive 2n-th root (its
+        # inverse table comes from the reference's per-entry extended Euclid)
+        (2, 17, 4),
+        (8192, _ntt_prime(8192, 1 << 31, down=True), None),
+        (1 << 17, _ntt_prime(1 << 17, 1 << 60, down=True), None),
+        (1 << 22, _ntt_prime(1 << 22, 1 << 60, down=True), None),
+        (16, 2251799813685313, 3),
     ]
     out = []
     for n, q, w in sets:
