@@ -27,6 +27,8 @@ the device so that a profiler capture of one launch ends quickly.
                 k_ntt_fwd<14,..,Mod63>, k_ntt_fwd_cluster<2, Shape<14,32,1,Mod63>>
   ntt_operand   256 polymuls of n = 2^14 with b given as NTT(b)  k_polymul<14,..,true> (the
                 epilogue instantiation, no steps)
+  lift_jobs     32 inverse transforms of n = 2^20 with a two-step centred lift
+                k_inv_global, k_ntt_inv<14,..>, k_lift_jobs (the epilogue pass)
   single_call_n65536  one polymul and one forward transform of n = 2^16 as single calls
                 k_polymul_cluster<4, Shape<12,16>>, k_ntt_fwd_cluster<4, ..> (16-CTA clusters)
 """
@@ -214,6 +216,22 @@ def case_wide_transforms(ctx):
     f14, k14 = _wide_transform_batch(ctx, 1 << 14, 1024)
     f16, k16 = _wide_transform_batch(ctx, 1 << 16, 64)
     return (lambda: (f14(), f16())), (k14, k16)
+
+
+def case_lift_jobs(ctx):
+    """32 inverse transforms of n = 2^20 (256 MB) with the centred-lift
+    epilogue: the global passes leave the words in HBM and k_lift_jobs
+    applies the steps (elemmod 65537, elemgtadd) as its own element-wise
+    pass."""
+    n, jobs, primes = 1 << 20, 32, 4
+    qs, tabs = _tabs(n, primes)
+    x = _operands(ctx, n, qs, jobs, 5)
+    y = vk.Vector(ctx, jobs * n)
+    bt = vk.Batch(ctx)
+    bt.add_transform([tabs[j % primes] for j in range(jobs)], x, y, inverse=True,
+                     lift=[("elemmod", 65537, 0), ("elemgtadd", 32768, 1 << 40)])
+    bt.commit(graph=True)
+    return bt.launch, (bt, x, y, tabs)
 
 
 def _wide_transform_batch(ctx, n, jobs, primes=8):

@@ -367,31 +367,87 @@ extern "C" int vkcu_polymul(void* stream, const vkcu_poly_job* jobs, int njobs, 
 }
 
 // The epilogue as its own element-wise pass: over `len` words at p, or over
-// the n output words of each job (q from the job's twiddle set).
-__global__ void k_lift_range(u64* __restrict__ p, u64 len, u64 q, const __grid_constant__ vkcu_lift lift) {
-  const LiftRun lr(&lift, q);
-  for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < len; i += (u64)gridDim.x * blockDim.x)
-    p[i] = lr(p[i]);
+// the n output words of each job (q from the job's twiddle set).  Words move
+// as 16-byte pairs, two pairs per thread per round, software pipelined (the
+// next round's loads are issued before this round's four words walk the
+// step list together and are stored); a word before the first 16-byte
+// boundary and an odd last word are done alone, and a job whose output is
+// not 16-byte aligned word by word.  The grid is one wave of resident blocks.
+__device__ __forceinline__ void lift_pairs(u64* __restrict__ a, long lo, long hi, long stride, const LiftRun& lr) {
+  ulonglong2 x0 = make_ulonglong2(0, 0), x1 = x0;
+  if (lo < hi) x0 = ld2(a + 2 * lo);
+  if (lo + stride < hi) x1 = ld2(a + 2 * (lo + stride));
+  for (long p = lo; p < hi; p += 2 * stride) {
+    const long n0 = p + 2 * stride, n1 = n0 + stride;
+    ulonglong2 y0 = x0, y1 = x1;
+    if (n0 < hi) y0 = ld2(a + 2 * n0);
+    if (n1 < hi) y1 = ld2(a + 2 * n1);
+    u64 v[4] = {x0.x, x0.y, x1.x, x1.y};
+    lr.apply(v);
+    st2(a + 2 * p, v[0], v[1]);
+    if (p + stride < hi) st2(a + 2 * (p + stride), v[2], v[3]);
+    x0 = y0;
+    x1 = y1;
+  }
 }
 
-__global__ void k_lift_jobs(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one, int log_n,
-                            const __grid_constant__ vkcu_lift lift) {
-  const long n = 1L << log_n;
-  const long per = (n + gridDim.y - 1) / gridDim.y;  // words of a job per block row
-  for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
-    const vkcu_ntt_job job = fetch_job(jobs, one, w);
+__global__ void __launch_bounds__(256) k_lift_range(u64* __restrict__ p, u64 len, u64 q,
+                                                    const __grid_constant__ vkcu_lift lift) {
+  const LiftRun lr(&lift, q);
+  const u64 head = (reinterpret_cast<uintptr_t>(p) & 15) ? 1 : 0;
+  const bool first = blockIdx.x == 0 && threadIdx.x == 0;
+  if (head && len && first) p[0] = lr(p[0]);
+  u64* a = p + head;
+  const u64 rest = len > head ? len - head : 0;
+  lift_pairs(a, (long)(blockIdx.x * blockDim.x + threadIdx.x), (long)(rest >> 1), (long)gridDim.x * blockDim.x, lr);
+  if ((rest & 1) && first) a[rest - 1] = lr(a[rest - 1]);
+}
+
+// Block b takes one even-sized contiguous range of the jobs' words laid end
+// to end (job j's words are j n .. j n + n - 1), so it starts over at most
+// once per job boundary inside its range.
+__global__ void __launch_bounds__(256) k_lift_jobs(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
+                                                   int log_n, const __grid_constant__ vkcu_lift lift) {
+  const long n = 1L << log_n, total = (long)njobs << log_n;
+  const long per = ((total + gridDim.x - 1) / gridDim.x + 1) & ~1L;
+  long lo = (long)blockIdx.x * per;
+  const long hi = lo + per < total ? lo + per : total;
+  while (lo < hi) {
+    const int j = (int)(lo >> log_n);
+    const long end = ((long)(j + 1) << log_n) < hi ? ((long)(j + 1) << log_n) : hi;
+    const vkcu_ntt_job job = fetch_job(jobs, one, j);
     const LiftRun lr(&lift, load_tw(job.tw).q);
-    u64* out = reinterpret_cast<u64*>(job.out);
-    const long lo = (long)blockIdx.y * per, hi = lo + per < n ? lo + per : n;
-    for (long i = lo + threadIdx.x; i < hi; i += blockDim.x) out[i] = lr(out[i]);
+    u64* out = reinterpret_cast<u64*>(job.out) + (lo & (n - 1));
+    const long words = end - lo;
+    if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+      lift_pairs(out, threadIdx.x, words >> 1, blockDim.x, lr);
+      if ((words & 1) && threadIdx.x == 0) out[words - 1] = lr(out[words - 1]);
+    } else {
+      for (long i = threadIdx.x; i < words; i += blockDim.x) out[i] = lr(out[i]);
+    }
+    lo = end;
   }
+}
+
+template <auto kernel>
+static long resident_blocks(int sms) {
+  static const int per_sm = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, 256, 0) != cudaSuccess || b < 1) b = 1;
+    return b;
+  }();
+  return (long)(sms > 0 ? sms : 1) * per_sm;
 }
 
 extern "C" int vkcu_lift_range(void* stream, uint64_t* p, uint64_t len, uint64_t q, const vkcu_lift* lift) {
   if (!has_lift(lift) || len == 0) return 0;
   if (lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
-  uint64_t blocks = (len + 255) / 256;
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long blocks = (long)((len + 1023) / 1024);  // four words per thread per round
+  const long cap = resident_blocks<k_lift_range>(sms);
+  if (blocks > cap) blocks = cap;
   k_lift_range<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<u64*>(p), len, q, *lift);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
@@ -402,15 +458,10 @@ extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs,
   if (!has_lift(lift)) return 0;
   if (njobs < 1 || log_n > (uint32_t)kMaxLogN || lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
-  const long n = 1L << log_n;
-  const int threads = n < 256 ? (int)((n + 31) / 32 * 32) : 256;
-  const long want = (long)(sms > 0 ? sms : 1) * 8;
-  const int gx = njobs < want ? njobs : (int)want;
-  long gy = (want + gx - 1) / gx;  // split each job when there are few
-  const long max_gy = (n + threads - 1) / threads;
-  if (gy > max_gy) gy = max_gy;
-  k_lift_jobs<<<dim3((unsigned)gx, (unsigned)gy), threads, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n,
-                                                                                      *lift);
+  long blocks = (((long)njobs << log_n) + 1023) / 1024;
+  const long cap = resident_blocks<k_lift_jobs>(sms);
+  if (blocks > cap) blocks = cap;
+  k_lift_jobs<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n, *lift);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
 }

@@ -536,6 +536,27 @@ struct LiftRun {
     }
     return x;
   }
+  // K words through the steps together: one walk of the step list, K
+  // independent chains.
+  template <int K>
+  __device__ __forceinline__ void apply(u64 (&v)[K]) const {
+#pragma unroll
+    for (int s = 0; s < VKCU_MAX_LIFT; s++) {
+      if (s >= (int)L->count) break;
+      const vkcu_lift_step& st = L->step[s];
+      const u32 kind = st.kind & 0xff;
+      if (kind == VKCU_LIFT_MODTWO) {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = ref_modtwo(v[k], bound[s]);
+      } else if (kind == VKCU_LIFT_GTSUB) {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = ref_gtsub(v[k], bound[s], d[s], st.mod, st.mu, st.bits);
+      } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = ref_gtadd(v[k], bound[s], d[s]);
+      }
+    }
+  }
 };
 
 struct NoLift {
