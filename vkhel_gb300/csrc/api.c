@@ -544,7 +544,7 @@ static int inverse_impl(const struct vkhel_vector *a, struct vkhel_vector *res, 
 		e = vkcu_elemmulconst(ctx->stream, res->dev + from, res->dev + from, res->length - from, t->ninv, t->ninv_s,
 				t->q);
 	if (!e && res->length > from)
-		e = vkcu_lift_range(ctx->stream, res->dev + from, res->length - from, t->q, lp);
+		e = vkcu_lift_range(ctx->stream, res->dev + from, res->length - from, t->q, ctx->sms, lp);
 	return finish(ctx, e, "inverse_transform");
 }
 
@@ -671,7 +671,7 @@ static int polymul_impl(const struct vkhel_vector *a, const struct vkhel_vector 
 		/* forward is a no-op at n = 1 and inverse scales by 1 */
 		int e = vkcu_elemmul(ctx->stream, res->dev, a->dev, b->dev, 1, t->q, t->mu, t->qbits);
 		if (!e)
-			e = vkcu_lift_range(ctx->stream, res->dev, 1, t->q, lp);
+			e = vkcu_lift_range(ctx->stream, res->dev, 1, t->q, ctx->sms, lp);
 		return finish(ctx, e, "polymul");
 	}
 	uint64_t *scratch = b_ntt ? b->dev : res->dev;

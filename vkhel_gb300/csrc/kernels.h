@@ -176,7 +176,7 @@ int vkcu_polymul_lift(void *stream, const vkcu_poly_job *jobs, int njobs,
 		const vkcu_poly_job *one, uint32_t log_n, int wide, int sms, const vkcu_lift *lift, int b_ntt);
 /* The epilogue alone, in place on `len` words at p (modulus q for TABLE_Q
  * steps), or on the n output words of every job. */
-int vkcu_lift_range(void *stream, uint64_t *p, uint64_t len, uint64_t q, const vkcu_lift *lift);
+int vkcu_lift_range(void *stream, uint64_t *p, uint64_t len, uint64_t q, int sms, const vkcu_lift *lift);
 int vkcu_lift_jobs(void *stream, const vkcu_ntt_job *jobs, int njobs, const vkcu_ntt_job *one,
 		uint32_t log_n, int sms, const vkcu_lift *lift);
 /* c = c * scratch mod q for every job (both canonical forward-transform

@@ -439,12 +439,9 @@ static long resident_blocks(int sms) {
   return (long)(sms > 0 ? sms : 1) * per_sm;
 }
 
-extern "C" int vkcu_lift_range(void* stream, uint64_t* p, uint64_t len, uint64_t q, const vkcu_lift* lift) {
+extern "C" int vkcu_lift_range(void* stream, uint64_t* p, uint64_t len, uint64_t q, int sms, const vkcu_lift* lift) {
   if (!has_lift(lift) || len == 0) return 0;
   if (lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long blocks = (long)((len + 1023) / 1024);  // four words per thread per round
   const long cap = resident_blocks<k_lift_range>(sms);
   if (blocks > cap) blocks = cap;
