@@ -118,3 +118,28 @@ def test_lift_rejects_bad_steps(vk, ctx):
     for steps in ([("elemmod", 7, 0)] * 5, [("elemmod", 1, q)], [("elemgtsub", 1, 1, 0)], [(9, 1, 1, 1)]):
         with pytest.raises(vk.VkhelError):
             vk.polymul_lift(a, b, c, t, steps)
+
+
+@pytest.mark.parametrize("log_n,jobs", [(1, 300), (5, 257), (7, 64), (11, 40), (18, 3)])
+def test_batched_inverse_lift_of_many_jobs(vk, ctx, oracle, log_n, jobs):
+    """A batch of inverse transforms with a lift on the multi-launch degrees
+    (n < 2^8: one block per job in the epilogue pass; 2^18: contiguous block
+    ranges across job boundaries) and a fused one (2^11), four primes
+    alternating, against the oracle's inverse followed by the ops."""
+    n = 1 << log_n
+    qs = workloads.ntt_primes(n, 4)
+    ws = [workloads.root_for(n, q) for q in qs]
+    tabs = [vk.NttTables(n, q, w) for q, w in zip(qs, ws)]
+    rng = np.random.default_rng(700 + log_n)
+    x_h = np.concatenate([workloads.uniform(rng, qs[j % 4], n) for j in range(jobs)])
+    x, y = vk.Vector(ctx, x_h), vk.Vector(ctx, jobs * n)
+    steps = [("elemmod", 65537, 0), ("elemgtadd", 1 << 15, 1 << 40)]
+    bt = vk.Batch(ctx)
+    bt.add_transform([tabs[j % 4] for j in range(jobs)], x, y, inverse=True, lift=steps)
+    bt.commit(graph=True)
+    bt.run()
+    got = y.download()
+    for j in range(jobs):
+        q, w = qs[j % 4], ws[j % 4]
+        ref = _apply(oracle, oracle.inverse(x_h[j * n:(j + 1) * n], n, q, w)[0], steps, q)
+        np.testing.assert_array_equal(got[j * n:(j + 1) * n], ref, err_msg=f"job {j}")

@@ -403,12 +403,34 @@ __global__ void __launch_bounds__(256) k_lift_range(u64* __restrict__ p, u64 len
   if ((rest & 1) && first) a[rest - 1] = lr(a[rest - 1]);
 }
 
-// Block b takes one even-sized contiguous range of the jobs' words laid end
-// to end (job j's words are j n .. j n + n - 1), so it starts over at most
-// once per job boundary inside its range.
+// Jobs of up to 2^11 words: one block per job (grid-stride over the jobs),
+// blockDim sized to the job.  Longer jobs: block b takes one even-sized
+// contiguous range of the jobs' words laid end to end (job j's words are
+// j n .. j n + n - 1), so it starts over at most once per job boundary
+// inside its range.
+static constexpr int kLiftSmallLog = 11;
+
+template <class L>
+__device__ __forceinline__ void lift_segment(u64* __restrict__ out, long words, const L& lr) {
+  if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    lift_pairs(out, threadIdx.x, words >> 1, blockDim.x, lr);
+    if ((words & 1) && threadIdx.x == 0) out[words - 1] = lr(out[words - 1]);
+  } else {
+    for (long i = threadIdx.x; i < words; i += blockDim.x) out[i] = lr(out[i]);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_lift_jobs(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
                                                    int log_n, const __grid_constant__ vkcu_lift lift) {
   const long n = 1L << log_n, total = (long)njobs << log_n;
+  if (log_n <= kLiftSmallLog) {
+    for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
+      const vkcu_ntt_job job = fetch_job(jobs, one, w);
+      const LiftRun lr(&lift, load_tw(job.tw).q);
+      lift_segment(reinterpret_cast<u64*>(job.out), n, lr);
+    }
+    return;
+  }
   const long per = ((total + gridDim.x - 1) / gridDim.x + 1) & ~1L;
   long lo = (long)blockIdx.x * per;
   const long hi = lo + per < total ? lo + per : total;
@@ -417,14 +439,7 @@ __global__ void __launch_bounds__(256) k_lift_jobs(const vkcu_ntt_job* __restric
     const long end = ((long)(j + 1) << log_n) < hi ? ((long)(j + 1) << log_n) : hi;
     const vkcu_ntt_job job = fetch_job(jobs, one, j);
     const LiftRun lr(&lift, load_tw(job.tw).q);
-    u64* out = reinterpret_cast<u64*>(job.out) + (lo & (n - 1));
-    const long words = end - lo;
-    if ((reinterpret_cast<uintptr_t>(out) & 15) == 0) {
-      lift_pairs(out, threadIdx.x, words >> 1, blockDim.x, lr);
-      if ((words & 1) && threadIdx.x == 0) out[words - 1] = lr(out[words - 1]);
-    } else {
-      for (long i = threadIdx.x; i < words; i += blockDim.x) out[i] = lr(out[i]);
-    }
+    lift_segment(reinterpret_cast<u64*>(job.out) + (lo & (n - 1)), end - lo, lr);
     lo = end;
   }
 }
@@ -455,10 +470,19 @@ extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs,
   if (!has_lift(lift)) return 0;
   if (njobs < 1 || log_n > (uint32_t)kMaxLogN || lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
-  long blocks = (((long)njobs << log_n) + 1023) / 1024;
-  const long cap = resident_blocks<k_lift_jobs>(sms);
-  if (blocks > cap) blocks = cap;
-  k_lift_jobs<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n, *lift);
+  int threads = 256;
+  long blocks;
+  if ((int)log_n <= kLiftSmallLog) {  // one block per job, a thread per pair up to 256
+    const long pairs = (1L << log_n) / 2;
+    threads = pairs <= 32 ? 32 : pairs >= 256 ? 256 : (int)pairs;
+    const long cap = (long)(sms > 0 ? sms : 1) * 16;
+    blocks = njobs < cap ? njobs : cap;
+  } else {
+    blocks = (((long)njobs << log_n) + 1023) / 1024;
+    const long cap = resident_blocks<k_lift_jobs>(sms);
+    if (blocks > cap) blocks = cap;
+  }
+  k_lift_jobs<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n, *lift);
   vkcu_count_launches(1);
   return (int)cudaGetLastError();
 }
