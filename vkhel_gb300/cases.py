@@ -28,7 +28,7 @@ the device so that a profiler capture of one launch ends quickly.
   ntt_operand   256 polymuls of n = 2^14 with b given as NTT(b)  k_polymul<14,..,true> (the
                 epilogue instantiation, no steps)
   lift_jobs     32 inverse transforms of n = 2^20 with a two-step centred lift
-                k_inv_global, k_ntt_inv<14,..>, k_lift_jobs (the epilogue pass)
+                k_inv_global, k_ntt_inv<14,..>, k_lift_stream (the epilogue pass)
   single_call_n65536  one polymul and one forward transform of n = 2^16 as single calls
                 k_polymul_cluster<4, Shape<12,16>>, k_ntt_fwd_cluster<4, ..> (16-CTA clusters)
 """
@@ -220,7 +220,7 @@ def case_wide_transforms(ctx):
 
 def case_lift_jobs(ctx):
     """32 inverse transforms of n = 2^20 (256 MB) with the centred-lift
-    epilogue: the global passes leave the words in HBM and k_lift_jobs
+    epilogue: the global passes leave the words in HBM and k_lift_stream
     applies the steps (elemmod 65537, elemgtadd) as its own element-wise
     pass."""
     n, jobs, primes = 1 << 20, 32, 4

@@ -521,6 +521,14 @@ struct LiftRun {
                                                                               : st.d;
     }
   }
+  // From constants resolved earlier (bound[], d[] of a LiftRun built for q).
+  __device__ __forceinline__ LiftRun(const vkcu_lift* l, const u64* b, const u64* dd) : L(l) {
+#pragma unroll
+    for (int s = 0; s < VKCU_MAX_LIFT; s++) {
+      bound[s] = b[s];
+      d[s] = dd[s];
+    }
+  }
   __device__ __forceinline__ u64 operator()(u64 x) const {
 #pragma unroll
     for (int s = 0; s < VKCU_MAX_LIFT; s++) {
