@@ -404,11 +404,7 @@ __global__ void __launch_bounds__(256) k_lift_range(u64* __restrict__ p, u64 len
 }
 
 // Jobs of up to 2^11 words: one block per job (grid-stride over the jobs),
-// blockDim sized to the job.  Longer jobs beyond what k_lift_stream stages:
-// block b takes one even-sized contiguous range of the jobs' words laid end
-// to end (job j's words are j n .. j n + n - 1), so it starts over at most
-// once per job boundary inside its range (0.71 of HBM against k_lift_stream's
-// 0.92 on 32 jobs of 2^20 words: 608 blocks streaming from 608 places).
+// blockDim sized to the job; longer jobs take k_lift_stream below.
 static constexpr int kLiftSmallLog = 11;
 
 template <class L>
@@ -423,34 +419,22 @@ __device__ __forceinline__ void lift_segment(u64* __restrict__ out, long words, 
 
 __global__ void __launch_bounds__(256) k_lift_jobs(const vkcu_ntt_job* __restrict__ jobs, int njobs, vkcu_ntt_job one,
                                                    int log_n, const __grid_constant__ vkcu_lift lift) {
-  const long n = 1L << log_n, total = (long)njobs << log_n;
-  if (log_n <= kLiftSmallLog) {
-    for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
-      const vkcu_ntt_job job = fetch_job(jobs, one, w);
-      const LiftRun lr(&lift, load_tw(job.tw).q);
-      lift_segment(reinterpret_cast<u64*>(job.out), n, lr);
-    }
-    return;
-  }
-  const long per = ((total + gridDim.x - 1) / gridDim.x + 1) & ~1L;
-  long lo = (long)blockIdx.x * per;
-  const long hi = lo + per < total ? lo + per : total;
-  while (lo < hi) {
-    const int j = (int)(lo >> log_n);
-    const long end = ((long)(j + 1) << log_n) < hi ? ((long)(j + 1) << log_n) : hi;
-    const vkcu_ntt_job job = fetch_job(jobs, one, j);
+  for (int w = blockIdx.x; w < njobs; w += gridDim.x) {
+    const vkcu_ntt_job job = fetch_job(jobs, one, w);
     const LiftRun lr(&lift, load_tw(job.tw).q);
-    lift_segment(reinterpret_cast<u64*>(job.out) + (lo & (n - 1)), end - lo, lr);
-    lo = end;
+    lift_segment(reinterpret_cast<u64*>(job.out), 1L << log_n, lr);
   }
 }
 
-// Long jobs (n >= 2^12), at most kLiftStreamJobs of them, 16-byte aligned:
-// the jobs' words laid end to end are walked in 128-word warp chunks, chunk
-// c by warp c mod W (W warps in the grid), so that the whole grid streams
-// through adjacent memory at any time; each job's output pointer and step
-// constants are staged in shared memory once per block.  Two pairs per lane
-// per chunk, the next chunk's loads issued before this chunk is lifted.
+// Long jobs (n >= 2^12), up to kLiftStreamJobs per launch: the jobs' words
+// laid end to end are walked in 128-word warp chunks, chunk c by warp c mod W
+// (W warps in the grid), so that the whole grid streams through adjacent
+// memory at any time (a block per contiguous range, 608 blocks reading from
+// 608 places, reached 0.71 of HBM against 0.91 so on 32 jobs of 2^20
+// words); each job's output pointer and step constants are staged in shared
+// memory once per block.  Two pairs per lane per chunk, the next chunk's
+// loads issued before this chunk is lifted; word by word when an output is
+// off the 16-byte grid.
 static constexpr int kLiftStreamJobs = 256;
 
 __global__ void __launch_bounds__(256) k_lift_stream(const vkcu_ntt_job* __restrict__ jobs, int njobs,
@@ -543,28 +527,27 @@ extern "C" int vkcu_lift_jobs(void* stream, const vkcu_ntt_job* jobs, int njobs,
   if (!has_lift(lift)) return 0;
   if (njobs < 1 || log_n > (uint32_t)kMaxLogN || lift->count > VKCU_MAX_LIFT) return (int)cudaErrorInvalidValue;
   const vkcu_ntt_job o = one ? *one : vkcu_ntt_job{};
-  int threads = 256;
-  long blocks;
   if ((int)log_n <= kLiftSmallLog) {  // one block per job, a thread per pair up to 256
     const long pairs = (1L << log_n) / 2;
-    threads = pairs <= 32 ? 32 : pairs >= 256 ? 256 : (int)pairs;
+    const int threads = pairs <= 32 ? 32 : pairs >= 256 ? 256 : (int)pairs;
     const long cap = (long)(sms > 0 ? sms : 1) * 16;
-    blocks = njobs < cap ? njobs : cap;
-  } else if (njobs <= kLiftStreamJobs) {
-    blocks = (((long)njobs << log_n) + 1023) / 1024;
-    const long cap = resident_blocks<k_lift_stream>(sms);
-    if (blocks > cap) blocks = cap;
-    k_lift_stream<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n, *lift);
+    const long blocks = njobs < cap ? njobs : cap;
+    k_lift_jobs<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n, *lift);
     vkcu_count_launches(1);
     return (int)cudaGetLastError();
-  } else {
-    blocks = (((long)njobs << log_n) + 1023) / 1024;
-    const long cap = resident_blocks<k_lift_jobs>(sms);
-    if (blocks > cap) blocks = cap;
   }
-  k_lift_jobs<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(jobs, njobs, o, (int)log_n, *lift);
-  vkcu_count_launches(1);
-  return (int)cudaGetLastError();
+  // long jobs: one streaming launch per kLiftStreamJobs jobs (a single job by value: one)
+  for (int g = 0; g < njobs; g += kLiftStreamJobs) {
+    const int cnt = njobs - g < kLiftStreamJobs ? njobs - g : kLiftStreamJobs;
+    long blocks = (((long)cnt << log_n) + 1023) / 1024;
+    const long cap = resident_blocks<k_lift_stream>(sms);
+    if (blocks > cap) blocks = cap;
+    k_lift_stream<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(jobs ? jobs + g : nullptr, cnt, o, (int)log_n,
+                                                                     *lift);
+    vkcu_count_launches(1);
+    if (const int e = (int)cudaGetLastError()) return e;
+  }
+  return 0;
 }
 
 // Pointwise step of a composed polymul: c = c * scratch mod q over njobs
